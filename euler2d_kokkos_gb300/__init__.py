@@ -1,0 +1,326 @@
+"""GB300-native unsplit MUSCL-Hancock Godunov step of euler2d_kokkos.
+
+Python front end of the C ABI in include/e2d.h (libe2d_gb300.so, built
+in-tree by euler2d_kokkos_gb300/build.py).  It mirrors the reference's
+driver interface:
+
+    params = HydroParams.from_ini("test_implode.ini")    # ConfigMap + HydroParams::setup
+    hydro  = HydroRun(params)                              # HydroRun<device>(params, configMap)
+    dt     = hydro.compute_dt(nStep % 2)
+    hydro.godunov_unsplit(nStep, dt)
+
+and adds the device-resident time loop (`step_n`).  All computation runs in
+hand-written sm_103a kernels; there is no CPU fallback: importing this module
+fails if the library cannot be loaded.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["HydroParams", "HydroRun", "E2DError", "load_library", "ID", "IP", "IE", "IU", "IV",
+           "RIEMANN", "BC_REFLECT", "BC_ABSORB", "BC_PERIODIC", "PROBLEMS", "PRECISION_FP64",
+           "PRECISION_FP32C"]
+
+ID, IP, IE, IU, IV = 0, 1, 1, 2, 3
+RIEMANN = {"approx": 0, "hll": 1, "hllc": 2}
+BC_REFLECT, BC_ABSORB, BC_PERIODIC = 1, 2, 3
+PROBLEMS = {"implode": 0, "blast": 1, "four_quadrant": 2, "discontinuity": 3, "shocked_bubble": 4}
+PRECISION_FP64, PRECISION_FP32C = 0, 1
+LAYOUT_LEFT, LAYOUT_RIGHT = 0, 1
+
+STATUS = {0: "E2D_OK", 1: "E2D_EINVAL", 2: "E2D_ENOMEM", 3: "E2D_ENUMERIC", 4: "E2D_ETIMEOUT",
+          5: "E2D_ECUDA", 6: "E2D_EIO"}
+
+
+class E2DError(RuntimeError):
+    """A non-zero e2d_status from the library."""
+
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        msg = f"{where}: {STATUS.get(status, status)}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+
+
+class _Params(ctypes.Structure):
+    # field order of struct e2d_params (include/e2d.h)
+    _fields_ = [
+        ("nStepmax", ctypes.c_int), ("tEnd", ctypes.c_double), ("nOutput", ctypes.c_int),
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("ghostWidth", ctypes.c_int),
+        ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
+        ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
+        ("boundary_type_xmin", ctypes.c_int), ("boundary_type_xmax", ctypes.c_int),
+        ("boundary_type_ymin", ctypes.c_int), ("boundary_type_ymax", ctypes.c_int),
+        ("gamma0", ctypes.c_double), ("cfl", ctypes.c_double), ("slope_type", ctypes.c_double),
+        ("smallr", ctypes.c_double), ("smallc", ctypes.c_double),
+        ("niter_riemann", ctypes.c_int), ("riemannSolverType", ctypes.c_int),
+        ("problemType", ctypes.c_int),
+        ("blast_radius", ctypes.c_double), ("blast_center_x", ctypes.c_double),
+        ("blast_center_y", ctypes.c_double), ("blast_density_in", ctypes.c_double),
+        ("blast_density_out", ctypes.c_double), ("blast_pressure_in", ctypes.c_double),
+        ("blast_pressure_out", ctypes.c_double), ("blast_total_energy_inside", ctypes.c_double),
+        ("bubble_radius", ctypes.c_double), ("bubble_center_x", ctypes.c_double),
+        ("bubble_center_y", ctypes.c_double), ("bubble_density", ctypes.c_double),
+        ("bubble_pressure", ctypes.c_double), ("preshock_density", ctypes.c_double),
+        ("preshock_pressure", ctypes.c_double), ("postshock_density", ctypes.c_double),
+        ("postshock_pressure", ctypes.c_double), ("postshock_velocity", ctypes.c_double),
+        ("shock_loc", ctypes.c_double),
+        ("fq_split_x", ctypes.c_double), ("fq_split_y", ctypes.c_double),
+        ("implode_shape", ctypes.c_int),
+        ("implementationVersion", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("imin", ctypes.c_int), ("imax", ctypes.c_int), ("jmin", ctypes.c_int),
+        ("jmax", ctypes.c_int), ("isize", ctypes.c_int), ("jsize", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("smallp", ctypes.c_double),
+        ("smallpp", ctypes.c_double), ("gamma6", ctypes.c_double),
+    ]
+
+
+# Every symbol declared in include/e2d.h, with its ctypes signature.
+_P = ctypes.POINTER(_Params)
+_V = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+SIGNATURES = {
+    "e2d_abi_version": ([], _I),
+    "e2d_status_string": ([_I], ctypes.c_char_p),
+    "e2d_params_defaults": ([_P], _I),
+    "e2d_params_from_ini": ([ctypes.c_char_p, _P], _I),
+    "e2d_params_init": ([_P], _I),
+    "e2d_create": ([_P, ctypes.POINTER(_V)], _I),
+    "e2d_destroy": ([_V], _I),
+    "e2d_last_error": ([_V], ctypes.c_char_p),
+    "e2d_get_params": ([_V, _P], _I),
+    "e2d_init_problem": ([_V], _I),
+    "e2d_set_state": ([_V, _I, _V, _I], _I),
+    "e2d_get_state": ([_V, _I, _V, _I], _I),
+    "e2d_device_state": ([_V, _I, ctypes.POINTER(_V)], _I),
+    "e2d_get_stream": ([_V, ctypes.POINTER(_V)], _I),
+    "e2d_make_boundaries": ([_V, _I], _I),
+    "e2d_compute_dt": ([_V, _I, ctypes.POINTER(_D)], _I),
+    "e2d_godunov_unsplit": ([_V, _I, _D], _I),
+    "e2d_step_n": ([_V, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I), _V], _I),
+    "e2d_set_profiling": ([_V, _I], _I),
+    "e2d_kernel_times": ([_V, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D),
+                          ctypes.POINTER(ctypes.c_long), ctypes.POINTER(_I)], _I),
+    "e2d_reset_kernel_times": ([_V], _I),
+}
+
+_lib = None
+
+
+def load_library(path: str | None = None, build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load libe2d_gb300.so (building it first if it is absent) and bind
+    every entry point of include/e2d.h.  Raises if anything is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    so = path or _build.LIB
+    if not os.path.exists(so):
+        if not build_if_missing:
+            raise OSError(f"{so} not found; run euler2d_kokkos_gb300/build.py")
+        _build.build()
+    L = ctypes.CDLL(so)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(L, name)  # AttributeError if the library lacks a symbol
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(status: int, where: str, sim=None):
+    if status != 0:
+        detail = ""
+        if sim is not None:
+            detail = (load_library().e2d_last_error(sim) or b"").decode()
+        raise E2DError(status, where, detail)
+
+
+class HydroParams:
+    """HydroParams + HydroSettings (src/HydroParams.h:107-265) as the flat
+    e2d_params struct.  Attribute access reads/writes the struct fields."""
+
+    def __init__(self, raw: _Params | None = None):
+        object.__setattr__(self, "_raw", raw if raw is not None else _Params())
+        if raw is None:
+            load_library().e2d_params_defaults(ctypes.byref(self._raw))
+
+    @classmethod
+    def from_ini(cls, path: str) -> "HydroParams":
+        """ConfigMap(path) followed by HydroParams::setup (reals go through float)."""
+        p = cls()
+        _check(load_library().e2d_params_from_ini(os.fsencode(path), ctypes.byref(p._raw)),
+               f"params_from_ini({path})")
+        return p
+
+    def init(self) -> "HydroParams":
+        """HydroParams::init: derived sizes and cut-offs, with validation."""
+        _check(load_library().e2d_params_init(ctypes.byref(self._raw)), "params_init")
+        return self
+
+    def copy(self) -> "HydroParams":
+        raw = _Params()
+        ctypes.memmove(ctypes.byref(raw), ctypes.byref(self._raw), ctypes.sizeof(_Params))
+        return HydroParams(raw)
+
+    def __getattr__(self, name):
+        return getattr(object.__getattribute__(self, "_raw"), name)
+
+    def __setattr__(self, name, value):
+        setattr(self._raw, name, value)
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self._raw, f) for f, _ in _Params._fields_}
+
+
+def make_params(nx, ny, *, problem="implode", riemann="hllc", gamma0=1.4, cfl=0.8,
+                slope_type=2.0, bc=(1, 1, 1, 1), xmin=0.0, xmax=1.0, ymin=0.0, ymax=1.0,
+                smallr=1e-10, smallc=1e-10, precision=PRECISION_FP64, float_params=True,
+                **extra) -> HydroParams:
+    """Parameters as HydroParams::setup would build them from an ini file
+    holding these values (with float_params, reals are rounded through float
+    like ConfigMap::getFloat)."""
+    import struct as _st
+
+    cv = (lambda x: _st.unpack("f", _st.pack("f", float(x)))[0]) if float_params else float
+    p = HydroParams()
+    p.nx, p.ny = int(nx), int(ny)
+    p.xmin, p.xmax, p.ymin, p.ymax = cv(xmin), cv(xmax), cv(ymin), cv(ymax)
+    (p.boundary_type_xmin, p.boundary_type_xmax,
+     p.boundary_type_ymin, p.boundary_type_ymax) = (int(b) for b in bc)
+    p.gamma0, p.cfl, p.slope_type = cv(gamma0), cv(cfl), cv(slope_type)
+    p.smallr, p.smallc = cv(smallr), cv(smallc)
+    p.riemannSolverType = RIEMANN[riemann] if isinstance(riemann, str) else int(riemann)
+    p.problemType = PROBLEMS[problem] if isinstance(problem, str) else int(problem)
+    p.precision = int(precision)
+    for k, v in extra.items():
+        setattr(p, k, cv(v) if isinstance(v, float) else v)
+    return p.init()
+
+
+class HydroRun:
+    """HydroRun<device> (src/HydroRun.h:44-134) on one GB300.
+
+    Owns U and U2 on the device.  `compute_dt`, `godunov_unsplit` and
+    `make_boundaries` follow the reference's methods; `U`/`U2` return host
+    copies shaped (4, jsize, isize) -- the reference's LayoutLeft memory
+    order with v = (rho, E, mx, my)."""
+
+    def __init__(self, params: HydroParams, init_problem: bool = True):
+        self._lib = load_library()
+        self.params = params.copy()
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_create(ctypes.byref(self.params._raw), ctypes.byref(h)), "e2d_create")
+        self._h = h
+        raw = _Params()
+        self._lib.e2d_get_params(self._h, ctypes.byref(raw))
+        self.params = HydroParams(raw)
+        self.shape = (4, self.params.jsize, self.params.isize)
+        if init_problem:
+            _check(self._lib.e2d_init_problem(self._h), "e2d_init_problem", self._h)
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- state transfer
+    def set_state(self, which: int, u: np.ndarray, layout: int = LAYOUT_LEFT):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.size != int(np.prod(self.shape)):
+            raise ValueError(f"state has {u.size} values, expected {int(np.prod(self.shape))}")
+        _check(self._lib.e2d_set_state(self._h, int(which), u.ctypes.data, layout), "e2d_set_state", self._h)
+
+    def get_state(self, which: int, out: np.ndarray | None = None, layout: int = LAYOUT_LEFT):
+        if out is None:
+            out = np.empty(self.shape if layout == LAYOUT_LEFT
+                           else (self.params.isize, self.params.jsize, 4), dtype=np.float64)
+        _check(self._lib.e2d_get_state(self._h, int(which), out.ctypes.data, layout), "e2d_get_state", self._h)
+        return out
+
+    @property
+    def U(self) -> np.ndarray:
+        return self.get_state(0)
+
+    @property
+    def U2(self) -> np.ndarray:
+        return self.get_state(1)
+
+    def device_state(self, which: int) -> int:
+        ptr = ctypes.c_void_p()
+        _check(self._lib.e2d_device_state(self._h, int(which), ctypes.byref(ptr)), "e2d_device_state")
+        return ptr.value
+
+    def stream(self) -> int:
+        ptr = ctypes.c_void_p()
+        _check(self._lib.e2d_get_stream(self._h, ctypes.byref(ptr)), "e2d_get_stream")
+        return ptr.value or 0
+
+    # -- the reference's methods
+    def make_boundaries(self, which: int):
+        _check(self._lib.e2d_make_boundaries(self._h, int(which)), "make_boundaries", self._h)
+
+    def compute_dt(self, useU: int) -> float:
+        dt = ctypes.c_double()
+        _check(self._lib.e2d_compute_dt(self._h, int(useU), ctypes.byref(dt)), "compute_dt", self._h)
+        return dt.value
+
+    def godunov_unsplit(self, nStep: int, dt: float):
+        _check(self._lib.e2d_godunov_unsplit(self._h, int(nStep), float(dt)), "godunov_unsplit", self._h)
+
+    # -- the device-resident time loop
+    def step_n(self, n: int, t_end: float, t: float, nstep: int, want_trace: bool = True):
+        """Up to n steps of the src/main.cpp loop on the device.
+        Returns (t, nstep, dt_trace)."""
+        tt = ctypes.c_double(t)
+        ns = ctypes.c_int(nstep)
+        trace = np.zeros(max(int(n), 1)) if want_trace else None
+        _check(self._lib.e2d_step_n(self._h, int(n), float(t_end), ctypes.byref(tt), ctypes.byref(ns),
+                                    trace.ctypes.data if trace is not None else None),
+               "step_n", self._h)
+        taken = ns.value - nstep
+        return tt.value, ns.value, (trace[:taken] if trace is not None else None)
+
+    def current(self, nstep: int) -> np.ndarray:
+        """State after nstep steps (U for even nstep, U2 for odd)."""
+        return self.get_state(nstep % 2)
+
+    # -- profiling
+    def set_profiling(self, on: bool):
+        _check(self._lib.e2d_set_profiling(self._h, int(bool(on))), "set_profiling")
+
+    def kernel_times(self) -> dict:
+        n = ctypes.c_int()
+        names = (ctypes.c_char_p * 16)()
+        ms = (ctypes.c_double * 16)()
+        cnt = (ctypes.c_long * 16)()
+        _check(self._lib.e2d_kernel_times(self._h, 16, names, ms, cnt, ctypes.byref(n)), "kernel_times")
+        return {names[k].decode(): (ms[k], cnt[k]) for k in range(min(n.value, 16))}
+
+    def reset_kernel_times(self):
+        self._lib.e2d_reset_kernel_times(self._h)

@@ -1,0 +1,439 @@
+// e2d_capi.cu -- the C ABI of include/e2d.h: simulation handles, device
+// buffers, the HydroRun method mirrors and the graph-replayed time loop.
+#include "e2d_internal.h"
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+using namespace e2d;
+
+struct e2d_sim {
+  e2d_params p{};
+  KParams64 kp{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  double *U[2] = {nullptr, nullptr};  // U and U2 of the reference
+  double *Q = nullptr;                // primitives scratch (one full array)
+  DevClock *clk = nullptr;            // device loop state
+  DevClock *clk_host = nullptr;       // pinned mirror
+  double *dt_trace = nullptr;         // device dt trace
+  int dt_trace_cap = 0;
+  std::string err;
+  // cached graphs: key = (steps << 1) | parity of the first input buffer
+  std::map<int, cudaGraphExec_t> graphs;
+  // per-kernel profiling
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::map<std::string, double> k_ms;
+  std::map<std::string, long> k_count;
+  std::vector<std::string> k_names;
+};
+
+namespace {
+
+constexpr int kGraphSteps = 8;  // steps captured per cached graph
+
+int set_err(e2d_sim *s, int status, const std::string &msg) {
+  if (s) s->err = msg;
+  return status;
+}
+
+int cuda_fail(e2d_sim *s, cudaError_t e, const char *what) {
+  if (e == cudaErrorMemoryAllocation)
+    return set_err(s, E2D_ENOMEM, std::string(what) + ": " + cudaGetErrorString(e));
+  return set_err(s, E2D_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define E2D_CK(sim, call, what)                     \
+  do {                                              \
+    cudaError_t e__ = (call);                       \
+    if (e__ != cudaSuccess) return cuda_fail(sim, e__, what); \
+  } while (0)
+
+void make_kparams(const e2d_params &p, KParams64 *kp) {
+  kp->g.nx = p.nx;
+  kp->g.ny = p.ny;
+  kp->g.isize = p.isize;
+  kp->g.jsize = p.jsize;
+  kp->g.plane = (long long)p.isize * p.jsize;
+  kp->g.bc_xmin = p.boundary_type_xmin;
+  kp->g.bc_xmax = p.boundary_type_xmax;
+  kp->g.bc_ymin = p.boundary_type_ymin;
+  kp->g.bc_ymax = p.boundary_type_ymax;
+  kp->ph.gamma0 = p.gamma0;
+  kp->ph.gamma6 = p.gamma6;
+  kp->ph.cfl = p.cfl;
+  kp->ph.slope_type = p.slope_type;
+  kp->ph.smallr = p.smallr;
+  kp->ph.smallc = p.smallc;
+  kp->ph.smallp = p.smallp;
+  kp->ph.smallpp = p.smallpp;
+  kp->ph.gm1 = p.gamma0 - 1.0;
+  kp->ph.entho = 1.0 / (p.gamma0 - 1.0);
+  kp->ph.smallc2 = p.smallc * p.smallc;
+  kp->ph.dx = p.dx;
+  kp->ph.dy = p.dy;
+}
+
+size_t state_count(const e2d_sim *s) { return (size_t)4 * s->p.isize * s->p.jsize; }
+
+// LayoutRight (OpenMP backend) <-> LayoutLeft (CUDA backend) on the host.
+void right_to_left(const e2d_params &p, const double *src, double *dst) {
+  const size_t plane = (size_t)p.isize * p.jsize;
+  for (int i = 0; i < p.isize; ++i)
+    for (int j = 0; j < p.jsize; ++j)
+      for (int v = 0; v < 4; ++v) dst[i + (size_t)p.isize * j + plane * v] = src[((size_t)i * p.jsize + j) * 4 + v];
+}
+void left_to_right(const e2d_params &p, const double *src, double *dst) {
+  const size_t plane = (size_t)p.isize * p.jsize;
+  for (int i = 0; i < p.isize; ++i)
+    for (int j = 0; j < p.jsize; ++j)
+      for (int v = 0; v < 4; ++v) dst[((size_t)i * p.jsize + j) * 4 + v] = src[i + (size_t)p.isize * j + plane * v];
+}
+
+// Kernels of one step of the device time loop, input buffer `par`.
+cudaError_t enqueue_step(e2d_sim *s, int par) {
+  double *in = s->U[par], *out = s->U[par ^ 1];
+  const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK;
+  cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream);
+  if (e != cudaSuccess) return e;
+  return launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 1, 0.0,
+                                s->dt_trace, s->stream);
+}
+
+cudaEvent_t pool_event(e2d_sim *s, size_t k) {
+  while (s->ev_pool.size() <= k) {
+    cudaEvent_t ev;
+    if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+    s->ev_pool.push_back(ev);
+  }
+  return s->ev_pool[k];
+}
+
+int get_graph(e2d_sim *s, int steps, int par, cudaGraphExec_t *out) {
+  const int key = (steps << 1) | par;
+  auto it = s->graphs.find(key);
+  if (it != s->graphs.end()) {
+    *out = it->second;
+    return E2D_OK;
+  }
+  cudaGraph_t graph;
+  E2D_CK(s, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture begin");
+  cudaError_t le = cudaSuccess;
+  for (int k = 0; k < steps && le == cudaSuccess; ++k) le = enqueue_step(s, (par + k) & 1);
+  cudaError_t ee = cudaStreamEndCapture(s->stream, &graph);
+  if (le != cudaSuccess) return cuda_fail(s, le, "capture step");
+  if (ee != cudaSuccess) return cuda_fail(s, ee, "capture end");
+  cudaGraphExec_t exec;
+  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ie != cudaSuccess) return cuda_fail(s, ie, "graph instantiate");
+  s->graphs[key] = exec;
+  *out = exec;
+  return E2D_OK;
+}
+
+int ensure_trace(e2d_sim *s, int n) {
+  if (n <= s->dt_trace_cap) return E2D_OK;
+  if (s->dt_trace) cudaFree(s->dt_trace);
+  s->dt_trace = nullptr;
+  s->dt_trace_cap = 0;
+  // the trace pointer is baked into captured graphs: drop them
+  for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  const int cap = n < 1024 ? 1024 : n;
+  E2D_CK(s, cudaMalloc(&s->dt_trace, sizeof(double) * cap), "dt trace alloc");
+  s->dt_trace_cap = cap;
+  return E2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int e2d_abi_version(void) { return E2D_ABI_VERSION; }
+
+const char *e2d_status_string(int status) {
+  switch (status) {
+    case E2D_OK: return "ok";
+    case E2D_EINVAL: return "invalid argument";
+    case E2D_ENOMEM: return "out of memory";
+    case E2D_ENUMERIC: return "numerical failure (NaN/Inf state or non-positive dt)";
+    case E2D_ETIMEOUT: return "device wait timed out";
+    case E2D_ECUDA: return "CUDA error";
+    case E2D_EIO: return "cannot read ini file";
+    default: return "unknown status";
+  }
+}
+
+int e2d_params_defaults(e2d_params *p) {
+  if (!p) return E2D_EINVAL;
+  params_defaults(p);
+  return E2D_OK;
+}
+
+int e2d_params_from_ini(const char *path, e2d_params *p) {
+  if (!path || !p) return E2D_EINVAL;
+  IniMap m;
+  const int rc = m.parse(path);
+  if (rc < 0) return E2D_EIO;
+  // like INIReader, a syntax error on some line still yields the keys parsed
+  return params_from_ini(m, p, nullptr);
+}
+
+int e2d_params_init(e2d_params *p) {
+  if (!p) return E2D_EINVAL;
+  return params_init(p, nullptr);
+}
+
+int e2d_create(const e2d_params *pin, e2d_sim **out) {
+  if (!pin || !out) return E2D_EINVAL;
+  *out = nullptr;
+  e2d_params p = *pin;
+  std::string msg;
+  int rc = params_init(&p, &msg);
+  if (rc != E2D_OK) return rc;
+  if (p.precision != E2D_PRECISION_FP64) return E2D_EINVAL;
+  e2d_sim *s = new (std::nothrow) e2d_sim();
+  if (!s) return E2D_ENOMEM;
+  s->p = p;
+  make_kparams(p, &s->kp);
+  auto fail = [&](int status) {
+    e2d_destroy(s);
+    return status;
+  };
+  if (cudaGetDevice(&s->device) != cudaSuccess) return fail(E2D_ECUDA);
+  if (configure_f64_kernels() != cudaSuccess) return fail(E2D_ECUDA);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(E2D_ECUDA);
+  const size_t bytes = sizeof(double) * state_count(s);
+  for (int k = 0; k < 2; ++k)
+    if (cudaMalloc(&s->U[k], bytes) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMalloc(&s->Q, bytes) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMalloc(&s->clk, sizeof(DevClock)) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMallocHost(&s->clk_host, sizeof(DevClock)) != cudaSuccess) return fail(E2D_ENOMEM);
+  std::memset(s->clk_host, 0, sizeof(DevClock));
+  if (cudaMemsetAsync(s->U[0], 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  if (cudaMemsetAsync(s->U[1], 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  if (cudaMemsetAsync(s->Q, 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  if (cudaMemsetAsync(s->clk, 0, sizeof(DevClock), s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  if (ensure_trace(s, 1024) != E2D_OK) return fail(E2D_ENOMEM);
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  *out = s;
+  return E2D_OK;
+}
+
+int e2d_destroy(e2d_sim *s) {
+  if (!s) return E2D_EINVAL;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto ev : s->ev_pool) cudaEventDestroy(ev);
+  for (int k = 0; k < 2; ++k)
+    if (s->U[k]) cudaFree(s->U[k]);
+  if (s->Q) cudaFree(s->Q);
+  if (s->clk) cudaFree(s->clk);
+  if (s->clk_host) cudaFreeHost(s->clk_host);
+  if (s->dt_trace) cudaFree(s->dt_trace);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return E2D_OK;
+}
+
+const char *e2d_last_error(const e2d_sim *s) { return s ? s->err.c_str() : "null handle"; }
+
+int e2d_get_params(const e2d_sim *s, e2d_params *p) {
+  if (!s || !p) return E2D_EINVAL;
+  *p = s->p;
+  return E2D_OK;
+}
+
+int e2d_get_stream(e2d_sim *s, void **stream) {
+  if (!s || !stream) return E2D_EINVAL;
+  *stream = (void *)s->stream;
+  return E2D_OK;
+}
+
+int e2d_device_state(e2d_sim *s, int which, double **dptr) {
+  if (!s || !dptr || (which != 0 && which != 1)) return E2D_EINVAL;
+  *dptr = s->U[which];
+  return E2D_OK;
+}
+
+int e2d_init_problem(e2d_sim *s) {
+  if (!s) return E2D_EINVAL;
+  E2D_CK(s, launch_init_f64(s->kp, s->p, s->U[0], s->stream), "init problem");
+  E2D_CK(s, cudaMemcpyAsync(s->U[1], s->U[0], sizeof(double) * state_count(s),
+                            cudaMemcpyDeviceToDevice, s->stream), "init copy");
+  E2D_CK(s, cudaStreamSynchronize(s->stream), "init sync");
+  return E2D_OK;
+}
+
+int e2d_set_state(e2d_sim *s, int which, const double *host, int layout) {
+  if (!s || !host || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad set_state args");
+  if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return set_err(s, E2D_EINVAL, "bad layout");
+  const size_t n = state_count(s);
+  if (layout == E2D_LAYOUT_LEFT) {
+    E2D_CK(s, cudaMemcpyAsync(s->U[which], host, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream), "set_state copy");
+  } else {
+    std::vector<double> tmp(n);
+    right_to_left(s->p, host, tmp.data());
+    E2D_CK(s, cudaMemcpyAsync(s->U[which], tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream), "set_state copy");
+    E2D_CK(s, cudaStreamSynchronize(s->stream), "set_state sync");
+    return E2D_OK;
+  }
+  E2D_CK(s, cudaStreamSynchronize(s->stream), "set_state sync");
+  return E2D_OK;
+}
+
+int e2d_get_state(e2d_sim *s, int which, double *host, int layout) {
+  if (!s || !host || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad get_state args");
+  if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return set_err(s, E2D_EINVAL, "bad layout");
+  const size_t n = state_count(s);
+  if (layout == E2D_LAYOUT_LEFT) {
+    E2D_CK(s, cudaMemcpyAsync(host, s->U[which], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
+    E2D_CK(s, cudaStreamSynchronize(s->stream), "get_state sync");
+  } else {
+    std::vector<double> tmp(n);
+    E2D_CK(s, cudaMemcpyAsync(tmp.data(), s->U[which], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
+    E2D_CK(s, cudaStreamSynchronize(s->stream), "get_state sync");
+    left_to_right(s->p, tmp.data(), host);
+  }
+  return E2D_OK;
+}
+
+int e2d_make_boundaries(e2d_sim *s, int which) {
+  if (!s || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad make_boundaries args");
+  E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_GHOSTS_IN, s->stream), "make_boundaries");
+  return E2D_OK;
+}
+
+int e2d_compute_dt(e2d_sim *s, int useU, double *dt) {
+  if (!s || !dt) return set_err(s, E2D_EINVAL, "bad compute_dt args");
+  const int which = (useU == 0) ? 0 : 1;
+  s->clk_host->invdt_bits = 0ull;
+  s->clk_host->status = 0u;
+  E2D_CK(s, cudaMemsetAsync(&s->clk->invdt_bits, 0, sizeof(unsigned long long), s->stream), "dt reset");
+  E2D_CK(s, cudaMemsetAsync(&s->clk->status, 0, sizeof(unsigned int), s->stream), "dt reset");
+  E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_DT, s->stream), "compute_dt");
+  E2D_CK(s, cudaMemcpyAsync(s->clk_host, s->clk, sizeof(DevClock), cudaMemcpyDeviceToHost, s->stream), "dt copy");
+  E2D_CK(s, cudaStreamSynchronize(s->stream), "dt sync");
+  double inv;
+  std::memcpy(&inv, &s->clk_host->invdt_bits, sizeof(double));
+  *dt = s->p.cfl / inv;  // src/HydroRun.h:248
+  if (s->clk_host->status & E2D_FLAG_NONFINITE) return set_err(s, E2D_ENUMERIC, "non-finite state value");
+  return E2D_OK;
+}
+
+int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
+  if (!s) return E2D_EINVAL;
+  const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
+  double *in = s->U[par], *out = s->U[par ^ 1];
+  const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT;
+  E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream), "godunov primitives");
+  E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 0, dt,
+                                   nullptr, s->stream), "godunov fluxes");
+  return E2D_OK;
+}
+
+int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *dt_trace) {
+  if (!s || !t || !nStep || n < 0) return set_err(s, E2D_EINVAL, "bad step_n args");
+  if (n == 0) return E2D_OK;
+  int rc = ensure_trace(s, n);
+  if (rc != E2D_OK) return rc;
+  DevClock c{};
+  c.t = *t;
+  c.t_end = t_end;
+  c.nstep = *nStep;
+  c.trace_base = *nStep;
+  c.trace_cap = n;
+  *s->clk_host = c;
+  E2D_CK(s, cudaMemcpyAsync(s->clk, s->clk_host, sizeof(DevClock), cudaMemcpyHostToDevice, s->stream), "clock upload");
+  const int par0 = (*nStep % 2 == 0) ? 0 : 1;
+  if (s->profiling) {
+    size_t ev = 0;
+    std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
+    const char *rs = s->p.riemannSolverType == E2D_RIEMANN_HLLC ? "hllc"
+                     : s->p.riemannSolverType == E2D_RIEMANN_HLL ? "hll" : "approx";
+    const std::string k2 = std::string("k_flux_update_f64<") + rs + ">";
+    for (int k = 0; k < n; ++k) {
+      const int par = (par0 + k) & 1;
+      double *in = s->U[par], *out = s->U[par ^ 1];
+      cudaEvent_t a = pool_event(s, ev++), b = pool_event(s, ev++), c2 = pool_event(s, ev++);
+      if (!a || !b || !c2) return set_err(s, E2D_ECUDA, "event create");
+      E2D_CK(s, cudaEventRecord(a, s->stream), "event");
+      E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk,
+                                FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK,
+                                s->stream), "fill");
+      E2D_CK(s, cudaEventRecord(b, s->stream), "event");
+      E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 1, 0.0,
+                                       s->dt_trace, s->stream), "flux");
+      E2D_CK(s, cudaEventRecord(c2, s->stream), "event");
+      marks.push_back({"k_fill_f64", {a, b}});
+      marks.push_back({k2, {b, c2}});
+    }
+    E2D_CK(s, cudaStreamSynchronize(s->stream), "profiled step sync");
+    for (auto &m : marks) {
+      float ms = 0.f;
+      E2D_CK(s, cudaEventElapsedTime(&ms, m.second.first, m.second.second), "event time");
+      if (!s->k_count.count(m.first)) s->k_names.push_back(m.first);
+      s->k_ms[m.first] += ms;
+      s->k_count[m.first] += 1;
+    }
+  } else {
+    int done = 0;
+    while (n - done >= kGraphSteps) {
+      cudaGraphExec_t g;
+      rc = get_graph(s, kGraphSteps, (par0 + done) & 1, &g);
+      if (rc != E2D_OK) return rc;
+      E2D_CK(s, cudaGraphLaunch(g, s->stream), "graph launch");
+      done += kGraphSteps;
+    }
+    for (; done < n; ++done) E2D_CK(s, enqueue_step(s, (par0 + done) & 1), "step launch");
+  }
+  E2D_CK(s, cudaMemcpyAsync(s->clk_host, s->clk, sizeof(DevClock), cudaMemcpyDeviceToHost, s->stream), "clock download");
+  E2D_CK(s, cudaStreamSynchronize(s->stream), "step_n sync");
+  const int taken = s->clk_host->nstep - *nStep;
+  if (dt_trace && taken > 0)
+    E2D_CK(s, cudaMemcpy(dt_trace, s->dt_trace, sizeof(double) * taken, cudaMemcpyDeviceToHost), "trace copy");
+  *t = s->clk_host->t;
+  *nStep = s->clk_host->nstep;
+  if (s->clk_host->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT))
+    return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
+                                                                              : "non-positive or non-finite dt");
+  return E2D_OK;
+}
+
+int e2d_set_profiling(e2d_sim *s, int on) {
+  if (!s) return E2D_EINVAL;
+  s->profiling = on != 0;
+  return E2D_OK;
+}
+
+int e2d_kernel_times(e2d_sim *s, int max_kernels, const char **names, double *ms, long *launches,
+                     int *n_kernels) {
+  if (!s || !n_kernels) return E2D_EINVAL;
+  int k = 0;
+  for (const auto &nm : s->k_names) {
+    if (k < max_kernels) {
+      if (names) names[k] = nm.c_str();
+      if (ms) ms[k] = s->k_ms[nm];
+      if (launches) launches[k] = s->k_count[nm];
+    }
+    ++k;
+  }
+  *n_kernels = k;
+  return E2D_OK;
+}
+
+int e2d_reset_kernel_times(e2d_sim *s) {
+  if (!s) return E2D_EINVAL;
+  s->k_ms.clear();
+  s->k_count.clear();
+  s->k_names.clear();
+  return E2D_OK;
+}
+
+}  // extern "C"

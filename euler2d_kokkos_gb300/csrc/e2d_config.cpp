@@ -1,0 +1,330 @@
+// e2d_config.cpp -- the reference's parameter contract on the host:
+// an ini reader with ConfigMap semantics (config/ConfigMap.{h,cpp},
+// config/inih/{ini,INIReader}.cpp) and HydroParams::setup / init
+// (src/HydroParams.cpp:42-190) filling the flat e2d_params of include/e2d.h.
+//
+// The behaviours that change numbers are kept on purpose:
+//  - reals are parsed with strtof and returned as float, so gamma0=1.4 is
+//    really (double)1.4f (config/ConfigMap.cpp:31-40), defaults included;
+//  - integers use strtol base 0 ("010" is 8; config/inih/INIReader.cpp:57-66);
+//  - keys are "section.name" lower-cased (config/inih/INIReader.cpp:92-100);
+//  - lines are read in 200-byte pieces, ';'/'#' start comments, an inline ';'
+//    after whitespace ends a value, and an indented line continues (replaces)
+//    the previous key's value (config/inih/ini.cpp:66-150).
+#include "e2d_internal.h"
+
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+
+namespace e2d {
+
+namespace {
+
+constexpr int kMaxLine = 200;
+constexpr int kMaxSection = 50;
+constexpr int kMaxName = 50;
+
+char *rstrip(char *s) {
+  char *p = s + std::strlen(s);
+  while (p > s && std::isspace(static_cast<unsigned char>(*--p))) *p = '\0';
+  return s;
+}
+
+char *lskip(char *s) {
+  while (*s && std::isspace(static_cast<unsigned char>(*s))) s++;
+  return s;
+}
+
+// First occurrence of c, or of a ';' that follows whitespace, or the end.
+char *find_char_or_comment(char *s, char c) {
+  bool was_space = false;
+  while (*s && *s != c && !(was_space && *s == ';')) {
+    was_space = std::isspace(static_cast<unsigned char>(*s)) != 0;
+    s++;
+  }
+  return s;
+}
+
+void copy_bounded(char *dst, const char *src, size_t size) {
+  std::strncpy(dst, src, size);
+  dst[size - 1] = '\0';
+}
+
+std::string make_key(const std::string &section, const std::string &name) {
+  std::string key = section + "." + name;
+  for (auto &ch : key) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+  return key;
+}
+
+}  // namespace
+
+int IniMap::parse(const char *path) {
+  FILE *f = std::fopen(path, "r");
+  if (!f) return -1;
+  char line[kMaxLine];
+  char section[kMaxSection] = "";
+  char prev_name[kMaxName] = "";
+  int lineno = 0, error = 0;
+  while (std::fgets(line, sizeof(line), f) != nullptr) {
+    lineno++;
+    char *start = lskip(rstrip(line));
+    if (*prev_name && *start && start > line) {
+      // indented non-blank line: a new value for the previous key
+      values_[make_key(section, prev_name)] = start;
+    } else if (*start == ';' || *start == '#') {
+      // comment line
+    } else if (*start == '[') {
+      char *end = find_char_or_comment(start + 1, ']');
+      if (*end == ']') {
+        *end = '\0';
+        copy_bounded(section, start + 1, sizeof(section));
+        *prev_name = '\0';
+      } else if (!error) {
+        error = lineno;
+      }
+    } else if (*start && *start != ';') {
+      char *end = find_char_or_comment(start, '=');
+      if (*end == '=') {
+        *end = '\0';
+        char *name = rstrip(start);
+        char *value = lskip(end + 1);
+        end = find_char_or_comment(value, '\0');
+        if (*end == ';') *end = '\0';
+        rstrip(value);
+        copy_bounded(prev_name, name, sizeof(prev_name));
+        values_[make_key(section, name)] = value;
+      } else if (!error) {
+        error = lineno;
+      }
+    }
+  }
+  std::fclose(f);
+  return error;
+}
+
+std::string IniMap::get_string(const std::string &section, const std::string &name,
+                               const std::string &dflt) const {
+  auto it = values_.find(make_key(section, name));
+  return it == values_.end() ? dflt : it->second;
+}
+
+long IniMap::get_integer(const std::string &section, const std::string &name, long dflt) const {
+  std::string s = get_string(section, name, "");
+  const char *v = s.c_str();
+  char *end = nullptr;
+  long n = std::strtol(v, &end, 0);
+  return end > v ? n : dflt;
+}
+
+float IniMap::get_float(const std::string &section, const std::string &name, float dflt) const {
+  std::string s = get_string(section, name, "");
+  const char *v = s.c_str();
+  char *end = nullptr;
+  float x = std::strtof(v, &end);
+  return end > v ? x : dflt;
+}
+
+bool IniMap::get_bool(const std::string &section, const std::string &name, bool dflt) const {
+  std::string s = get_string(section, name, "");
+  bool val = dflt;
+  if (s == "1" || s == "yes" || s == "true" || s == "on") val = true;
+  if (s == "0" || s == "no" || s == "false" || s == "off") val = false;
+  if (s.empty()) val = dflt;
+  return val;
+}
+
+// HydroParams() member defaults (src/HydroParams.h:222-258) and the
+// defaults HydroParams::setup passes to ConfigMap (src/HydroParams.cpp).
+void params_defaults(e2d_params *p) {
+  std::memset(p, 0, sizeof(*p));
+  p->nStepmax = 1000;
+  p->tEnd = 0.0;
+  p->nOutput = 100;
+  p->nx = 2;
+  p->ny = 2;
+  p->ghostWidth = 2;
+  p->xmin = 0.0;
+  p->xmax = 1.0;
+  p->ymin = 0.0;
+  p->ymax = 1.0;
+  p->boundary_type_xmin = p->boundary_type_xmax = E2D_BC_REFLECT;
+  p->boundary_type_ymin = p->boundary_type_ymax = E2D_BC_REFLECT;
+  p->gamma0 = (double)1.4f;
+  p->cfl = (double)0.5f;
+  p->slope_type = 1.0;
+  p->smallr = (double)1e-10f;
+  p->smallc = (double)1e-10f;
+  p->niter_riemann = 10;
+  p->riemannSolverType = E2D_RIEMANN_APPROX;
+  p->problemType = E2D_PROBLEM_IMPLODE;
+  p->blast_radius = (double)(float)(1.0 / 2.0 / 10);
+  p->blast_center_x = (double)0.5f;
+  p->blast_center_y = (double)0.5f;
+  p->blast_density_in = 1.0;
+  p->blast_density_out = (double)1.2f;
+  p->blast_pressure_in = 10.0;
+  p->blast_pressure_out = (double)0.1f;
+  p->blast_total_energy_inside = 0.0;
+  p->bubble_radius = (double)0.025f;
+  p->bubble_center_x = (double)0.225f;
+  p->bubble_center_y = (double)0.0445f;
+  p->bubble_density = (double)3.863f;
+  p->bubble_pressure = (double)1.0132e5f;
+  p->preshock_density = (double)1.225f;
+  p->preshock_pressure = (double)1.0132e5f;
+  p->postshock_density = (double)1.686f;
+  p->postshock_pressure = (double)1.59e5f;
+  p->postshock_velocity = (double)113.5f;
+  p->shock_loc = (double)0.170f;
+  p->fq_split_x = (double)0.8f;
+  p->fq_split_y = (double)0.8f;
+  p->implode_shape = 0;
+  p->implementationVersion = 0;
+  p->precision = E2D_PRECISION_FP64;
+}
+
+// src/HydroParams.cpp:42-156 (HydroParams::setup), then init().
+int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
+  params_defaults(p);
+  p->nStepmax = (int)m.get_integer("run", "nstepmax", 1000);
+  p->tEnd = m.get_float("run", "tend", 0.0f);
+  p->nOutput = (int)m.get_integer("run", "noutput", 100);
+
+  p->nx = (int)m.get_integer("mesh", "nx", 2);
+  p->ny = (int)m.get_integer("mesh", "ny", 2);
+  p->xmin = m.get_float("mesh", "xmin", 0.0f);
+  p->ymin = m.get_float("mesh", "ymin", 0.0f);
+  p->xmax = m.get_float("mesh", "xmax", 1.0f);
+  p->ymax = m.get_float("mesh", "ymax", 1.0f);
+  p->boundary_type_xmin = (int)m.get_integer("mesh", "boundary_type_xmin", E2D_BC_REFLECT);
+  p->boundary_type_xmax = (int)m.get_integer("mesh", "boundary_type_xmax", E2D_BC_REFLECT);
+  p->boundary_type_ymin = (int)m.get_integer("mesh", "boundary_type_ymin", E2D_BC_REFLECT);
+  p->boundary_type_ymax = (int)m.get_integer("mesh", "boundary_type_ymax", E2D_BC_REFLECT);
+
+  p->gamma0 = m.get_float("hydro", "gamma0", 1.4f);
+  p->cfl = m.get_float("hydro", "cfl", 0.5f);
+  p->slope_type = m.get_float("hydro", "slope_type", 1.0f);
+  p->smallc = m.get_float("hydro", "smallc", 1e-10f);
+  p->smallr = m.get_float("hydro", "smallr", 1e-10f);
+  p->niter_riemann = (int)m.get_integer("hydro", "niter_riemann", 10);
+
+  const std::string rs = m.get_string("hydro", "riemann", "approx");
+  if (rs == "approx")
+    p->riemannSolverType = E2D_RIEMANN_APPROX;
+  else if (rs == "hll")
+    p->riemannSolverType = E2D_RIEMANN_HLL;
+  else if (rs == "hllc")
+    p->riemannSolverType = E2D_RIEMANN_HLLC;
+  else {
+    // the reference prints a notice and falls back to approx (:100-105)
+    p->riemannSolverType = E2D_RIEMANN_APPROX;
+    if (msg) *msg += "riemann solver '" + rs + "' is invalid, using approx; ";
+  }
+
+  const std::string ps = m.get_string("hydro", "problem", "unknown");
+  if (ps == "implode")
+    p->problemType = E2D_PROBLEM_IMPLODE;
+  else if (ps == "blast")
+    p->problemType = E2D_PROBLEM_BLAST;
+  else if (ps == "four_quadrant")
+    p->problemType = E2D_PROBLEM_FOUR_QUADRANT;
+  else if (ps == "discontinuity")
+    p->problemType = E2D_PROBLEM_DISCONTINUITY;
+  else if (ps == "shocked_bubble")
+    p->problemType = E2D_PROBLEM_SHOCKED_BUBBLE;
+  else {
+    p->problemType = E2D_PROBLEM_IMPLODE;
+    if (msg) *msg += "problem '" + ps + "' is invalid, using implode; ";
+  }
+
+  // src/HydroParams.cpp:19-37 (readShockedBubbleParams)
+  p->bubble_radius = m.get_float("shocked_bubble", "bubble_radius", 0.025f);
+  p->bubble_center_x = m.get_float("shocked_bubble", "bubble_center_x", 0.225f);
+  p->bubble_center_y = m.get_float("shocked_bubble", "bubble_center_y", 0.0445f);
+  p->bubble_density = m.get_float("shocked_bubble", "bubble_density", 3.863f);
+  p->bubble_pressure = m.get_float("shocked_bubble", "bubble_pressure", 1.0132e5f);
+  p->preshock_density = m.get_float("shocked_bubble", "preshock_density", 1.225f);
+  p->preshock_pressure = m.get_float("shocked_bubble", "preshock_pressure", 1.0132e5f);
+  p->postshock_density = m.get_float("shocked_bubble", "postshock_density", 1.686f);
+  p->postshock_pressure = m.get_float("shocked_bubble", "postshock_pressure", 1.59e5f);
+  p->postshock_velocity = m.get_float("shocked_bubble", "postshock_velocity", 113.5f);
+  p->shock_loc = m.get_float("shocked_bubble", "shock_loc", 0.170f);
+
+  // defaults depend on the mesh, computed in double then narrowed to float
+  p->blast_radius = m.get_float("blast", "radius", (float)((p->xmin + p->xmax) / 2.0 / 10));
+  p->blast_center_x = m.get_float("blast", "center_x", (float)((p->xmin + p->xmax) / 2));
+  p->blast_center_y = m.get_float("blast", "center_y", (float)((p->ymin + p->ymax) / 2));
+  p->blast_density_in = m.get_float("blast", "density_in", 1.0f);
+  p->blast_density_out = m.get_float("blast", "density_out", 1.2f);
+  p->blast_pressure_in = m.get_float("blast", "pressure_in", 10.0f);
+  p->blast_pressure_out = m.get_float("blast", "pressure_out", 0.1f);
+  p->blast_total_energy_inside = m.get_float("blast", "total_energy_inside", 0.0f);
+
+  // extensions of this build (absent keys keep the reference's behaviour)
+  p->fq_split_x = m.get_float("four_quadrant", "split_x", 0.8f);
+  p->fq_split_y = m.get_float("four_quadrant", "split_y", 0.8f);
+  p->implode_shape = (int)m.get_integer("implode", "shape", 0);
+  const std::string prec = m.get_string("gb300", "precision", "fp64");
+  p->precision = (prec == "fp32c") ? E2D_PRECISION_FP32C : E2D_PRECISION_FP64;
+
+  // getFloat then an implicit float->int conversion (:149-155)
+  p->implementationVersion = (int)m.get_float("OTHER", "implementationVersion", 0.0f);
+  if (p->implementationVersion != 0 && p->implementationVersion != 1 &&
+      p->implementationVersion != 2) {
+    if (msg) *msg += "implementation version is invalid, using 0; ";
+    p->implementationVersion = 0;
+  }
+  return params_init(p, msg);
+}
+
+// src/HydroParams.cpp:160-190 (HydroParams::init) plus the validation the
+// GPU path needs (the reference exits or runs undefined code on these).
+int params_init(e2d_params *p, std::string *msg) {
+  if (p->ghostWidth != 2) {
+    if (msg) *msg += "ghostWidth must be 2; ";
+    return E2D_EINVAL;
+  }
+  p->imin = 0;
+  p->jmin = 0;
+  p->imax = p->nx - 1 + 2 * p->ghostWidth;
+  p->jmax = p->ny - 1 + 2 * p->ghostWidth;
+  p->isize = p->imax - p->imin + 1;
+  p->jsize = p->jmax - p->jmin + 1;
+  p->dx = (p->xmax - p->xmin) / p->nx;
+  p->dy = (p->ymax - p->ymin) / p->ny;
+  p->smallp = p->smallc * p->smallc / p->gamma0;
+  p->smallpp = p->smallr * p->smallp;
+  p->gamma6 = (p->gamma0 + 1.0) / (2.0 * p->gamma0);
+
+  auto bad = [&](const char *what) {
+    if (msg) *msg += std::string(what) + "; ";
+    return E2D_EINVAL;
+  };
+  if (p->nx < 1 || p->ny < 1) return bad("nx and ny must be >= 1");
+  if ((long long)p->isize * p->jsize >= (1LL << 31)) return bad("grid too large (isize*jsize >= 2^31)");
+  const int bcs[4] = {p->boundary_type_xmin, p->boundary_type_xmax, p->boundary_type_ymin,
+                      p->boundary_type_ymax};
+  for (int b : bcs)
+    if (b < E2D_BC_REFLECT || b > E2D_BC_PERIODIC) return bad("boundary_type must be 1, 2 or 3");
+  // every ghost cell must take its value from an interior cell, which needs
+  // an interior at least as wide as the ghost layer
+  if (p->nx < 2 || p->ny < 2) return bad("nx and ny must be >= 2 (ghost layer of 2)");
+  if (!(p->slope_type == 0.0 || p->slope_type == 1.0 || p->slope_type == 2.0))
+    return bad("slope_type must be 0, 1 or 2");
+  if (!(p->gamma0 > 1.0)) return bad("gamma0 must be > 1");
+  if (!(p->cfl > 0.0)) return bad("cfl must be > 0");
+  if (!(p->dx > 0.0) || !(p->dy > 0.0)) return bad("xmax > xmin and ymax > ymin required");
+  if (!(p->smallr > 0.0) || !(p->smallc > 0.0)) return bad("smallr and smallc must be > 0");
+  if (p->riemannSolverType < 0 || p->riemannSolverType > 2) return bad("riemann solver must be 0, 1 or 2");
+  if (p->precision != E2D_PRECISION_FP64 && p->precision != E2D_PRECISION_FP32C)
+    return bad("precision must be fp64 or fp32c");
+  if (p->problemType < 0 || p->problemType > 4) return bad("problem must be 0..4");
+  return E2D_OK;
+}
+
+}  // namespace e2d

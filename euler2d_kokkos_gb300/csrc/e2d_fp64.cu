@@ -1,0 +1,698 @@
+// e2d_fp64.cu -- FP64 kernels of the unsplit MUSCL-Hancock Godunov step,
+// bit-identical to the reference (compiled with --fmad=false; every
+// expression keeps the reference's operation order).
+//
+// One time step is two launches:
+//   k_fill_f64         ghost fill (make_boundaries, src/HydroRun.h:388-399)
+//                      into both states, primitives of every cell
+//                      (ConvertToPrimitivesFunctor, src/HydroRunFunctors.h:84-143)
+//                      and the CFL maximum of the interior
+//                      (ComputeDtFunctor, src/HydroRunFunctors.h:17-79);
+//   k_flux_update_f64  per 32x16 tile: limited slopes once per cell, the
+//                      half-step trace once per cell and face, one Riemann
+//                      solve per face, the conservative update
+//                      (ComputeAndStoreFluxesFunctor + UpdateFunctor,
+//                      src/HydroRunFunctors.h:412-723) and the time-loop
+//                      bookkeeping of src/main.cpp:128-143.
+// The reference evaluates the slopes of a cell three times and the trace
+// sources four times per cell; evaluating each once gives the same bits.
+#include "e2d_internal.h"
+
+#include <cstdint>
+
+namespace e2d {
+namespace {
+
+constexpr int TX = 32;        // interior cells per tile along x
+constexpr int TY = 16;        // interior cells per tile along y
+constexpr int QW = TX + 4;    // primitives tile width (2-cell halo)
+constexpr int QH = TY + 4;
+constexpr int XW = TX + 2;    // x-face states: cells x in [-1, TX]
+constexpr int YH = TY + 2;    // y-face states: cells y in [-1, TY]
+constexpr int NT = 256;       // threads per tile block
+constexpr int FILL_BX = 64, FILL_BY = 4;
+
+constexpr size_t kSmemDoubles = 4 * QH * QW + 2 * (4 * TY * XW) + 2 * (4 * YH * TX);
+
+// ------------------------------------------------------------ ghost map
+// Source cell of a ghost: the composition of the X-face pass (all rows) and
+// the Y-face pass (all columns) of MakeBoundariesFunctor
+// (src/HydroRunFunctors.h:1855-2024).  Reflect mirrors (2g-1-i) and flips
+// the normal momentum, absorb copies the first interior cell, periodic
+// wraps.  The result is always an interior cell (nx, ny >= 2).
+__device__ __forceinline__ int src_lo_hi(int i, int n, int bc_lo, int bc_hi, bool &flip) {
+  flip = false;
+  if (i < 2) {
+    if (bc_lo == E2D_BC_REFLECT) {
+      flip = true;
+      return 3 - i;
+    }
+    if (bc_lo == E2D_BC_ABSORB) return 2;
+    return n + i;
+  }
+  if (i >= n + 2) {
+    if (bc_hi == E2D_BC_REFLECT) {
+      flip = true;
+      return 2 * n + 3 - i;
+    }
+    if (bc_hi == E2D_BC_ABSORB) return n + 1;
+    return i - n;
+  }
+  return i;
+}
+
+__device__ __forceinline__ bool nonfinite(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
+}
+
+// ------------------------------------------------------------ numerics
+// src/HydroBaseFunctor.h:421-455, one direction.
+__device__ __forceinline__ double slope_1d(double st, double q, double qp, double qm) {
+  const double dlft = st * (q - qm);
+  const double drgt = st * (qp - q);
+  const double dcen = 0.5 * (qp - qm);
+  const double dsgn = (dcen >= 0.0) ? 1.0 : -1.0;
+  const double slop = fmin(fabs(dlft), fabs(drgt));
+  const double dlim = ((dlft * drgt) <= 0.0) ? 0.0 : slop;
+  return dsgn * fmin(dlim, fabs(dcen));
+}
+
+// src/HydroBaseFunctor.h:523-547.
+__device__ __forceinline__ void cmpflx(const KPhys<double> &ph, const double g[4], double f[4]) {
+  f[E2D_ID] = g[E2D_ID] * g[E2D_IU];
+  f[E2D_IU] = f[E2D_ID] * g[E2D_IU] + g[E2D_IP];
+  f[E2D_IV] = f[E2D_ID] * g[E2D_IV];
+  const double ekin = 0.5 * g[E2D_ID] * (g[E2D_IU] * g[E2D_IU] + g[E2D_IV] * g[E2D_IV]);
+  const double etot = g[E2D_IP] * ph.entho + ekin;
+  f[E2D_IP] = g[E2D_IU] * (etot + g[E2D_IP]);
+}
+
+// src/HydroBaseFunctor.h:558-693 (riemann_approx).
+__device__ __noinline__ void riemann_approx(const KPhys<double> &ph, const double *ql,
+                                            const double *qr, double *flux) {
+  const double gamma0 = ph.gamma0, gamma6 = ph.gamma6;
+  const double rl = fmax(ql[E2D_ID], ph.smallr), ul = ql[E2D_IU];
+  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
+  const double rr = fmax(qr[E2D_ID], ph.smallr), ur = qr[E2D_IU];
+  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
+  const double cl = gamma0 * pl * rl;
+  const double cr = gamma0 * pr * rr;
+  double wl = sqrt(cl);
+  double wr = sqrt(cr);
+  double pstar = fmax(((wr * pl + wl * pr) + wl * wr * (ul - ur)) / (wl + wr), 0.0);
+  double pold = pstar;
+  double conv = 1.0;
+  for (int iter = 0; (iter < 10) && (conv > 1e-6); ++iter) {
+    const double wwl = sqrt(cl * (1.0 + gamma6 * (pold - pl) / pl));
+    const double wwr = sqrt(cr * (1.0 + gamma6 * (pold - pr) / pr));
+    const double qxl = 2.0 * wwl * wwl * wwl / (wwl * wwl + cl);
+    const double qxr = 2.0 * wwr * wwr * wwr / (wwr * wwr + cr);
+    const double usl = ul - (pold - pl) / wwl;
+    const double usr = ur + (pold - pr) / wwr;
+    const double delp = fmax(qxr * qxl / (qxr + qxl) * (usl - usr), -pold);
+    pold = pold + delp;
+    conv = fabs(delp / (pold + ph.smallpp));
+  }
+  pstar = pold;
+  wl = sqrt(cl * (1.0 + gamma6 * (pstar - pl) / pl));
+  wr = sqrt(cr * (1.0 + gamma6 * (pstar - pr) / pr));
+  const double ustar = 0.5 * (ul + (pl - pstar) / wl + ur - (pr - pstar) / wr);
+  const double sgnm = copysign(1.0, ustar);
+  const bool lft = sgnm > 0.0;
+  const double ro = lft ? rl : rr, uo = lft ? ul : ur, po = lft ? pl : pr, wo = lft ? wl : wr;
+  const double co = fmax(ph.smallc, sqrt(fabs(gamma0 * po / ro)));
+  const double rstar = fmax((ro / (1.0 + ro * (po - pstar) / (wo * wo))), ph.smallr);
+  const double cstar = fmax(ph.smallc, sqrt(fabs(gamma0 * pstar / rstar)));
+  double spout = co - sgnm * uo;
+  double spin = cstar - sgnm * ustar;
+  const double ushock = wo / ro - sgnm * uo;
+  if (pstar >= po) {
+    spin = ushock;
+    spout = ushock;
+  }
+  const double scr = fmax(spout - spin, ph.smallc + fabs(spout + spin));
+  double frac = 0.5 * (1.0 + (spout + spin) / scr);
+  if (frac != frac)
+    frac = 0.0;
+  else
+    frac = frac >= 1.0 ? 1.0 : frac <= 0.0 ? 0.0 : frac;
+  double g[4];
+  g[E2D_ID] = frac * rstar + (1.0 - frac) * ro;
+  g[E2D_IU] = frac * ustar + (1.0 - frac) * uo;
+  g[E2D_IP] = frac * pstar + (1.0 - frac) * po;
+  if (spout < 0.0) {
+    g[E2D_ID] = ro;
+    g[E2D_IU] = uo;
+    g[E2D_IP] = po;
+  }
+  if (spin > 0.0) {
+    g[E2D_ID] = rstar;
+    g[E2D_IU] = ustar;
+    g[E2D_IP] = pstar;
+  }
+  g[E2D_IV] = lft ? ql[E2D_IV] : qr[E2D_IV];
+  cmpflx(ph, g, flux);
+}
+
+// src/HydroBaseFunctor.h:704-809 (riemann_hllc).  The reference builds the
+// star states of both sides and keeps one; this builds only the side the
+// contact selects (ustar > 0: left), which yields the same value.
+__device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const double *ql,
+                                             const double *qr, double *flux) {
+  const double rl = fmax(ql[E2D_ID], ph.smallr);
+  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
+  const double ul = ql[E2D_IU];
+  double ecinl = 0.5 * rl * ul * ul;
+  ecinl = ecinl + 0.5 * rl * ql[E2D_IV] * ql[E2D_IV];
+  const double etotl = pl * ph.entho + ecinl;
+  const double rr = fmax(qr[E2D_ID], ph.smallr);
+  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
+  const double ur = qr[E2D_IU];
+  double ecinr = 0.5 * rr * ur * ur;
+  ecinr = ecinr + 0.5 * rr * qr[E2D_IV] * qr[E2D_IV];
+  const double etotr = pr * ph.entho + ecinr;
+  const double cfastl = sqrt(fmax(ph.gamma0 * pl / rl, ph.smallc2));
+  const double cfastr = sqrt(fmax(ph.gamma0 * pr / rr, ph.smallc2));
+  const double cmax = fmax(cfastl, cfastr);
+  const double SL = fmin(ul, ur) - cmax;
+  const double SR = fmax(ul, ur) + cmax;
+  const double rcl = rl * (ul - SL);
+  const double rcr = rr * (SR - ur);
+  const double ustar = (rcr * ur + rcl * ul + (pl - pr)) / (rcr + rcl);
+  const double ptotstar = (rcr * pl + rcl * pr + rcl * rcr * (ul - ur)) / (rcr + rcl);
+  const bool lft = ustar > 0.0;
+  const double S = lft ? SL : SR;
+  const double rs = lft ? rl : rr, us = lft ? ul : ur, ps = lft ? pl : pr;
+  const double es = lft ? etotl : etotr;
+  const double sdu = S - us;
+  const double sds = S - ustar;
+  const double rstar = rs * sdu / sds;
+  const double etotstar = (sdu * es - ps * us + ptotstar * ustar) / sds;
+  double ro, uo, ptoto, etoto;
+  if (SL > 0.0) {
+    ro = rl, uo = ul, ptoto = pl, etoto = etotl;
+  } else if (lft || SR > 0.0) {
+    ro = rstar, uo = ustar, ptoto = ptotstar, etoto = etotstar;
+  } else {
+    ro = rr, uo = ur, ptoto = pr, etoto = etotr;
+  }
+  flux[E2D_ID] = ro * uo;
+  flux[E2D_IU] = flux[E2D_ID] * uo + ptoto;
+  flux[E2D_IP] = (etoto + ptoto) * uo;
+  flux[E2D_IV] = (flux[E2D_ID] > 0.0) ? flux[E2D_ID] * ql[E2D_IV] : flux[E2D_ID] * qr[E2D_IV];
+}
+
+// HLL flux (Harten, Lax, van Leer; Toro, "Riemann Solvers and Numerical
+// Methods for Fluid Dynamics", 3rd ed., eq. 10.21).  The reference declares
+// RIEMANN_HLL but has no solver; this uses riemann_hllc's cut-offs and Davis
+// wave speeds.  Operation order matches the oracle's riemann_hll.
+__device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const double *ql,
+                                            const double *qr, double *flux) {
+  const double rl = fmax(ql[E2D_ID], ph.smallr);
+  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
+  const double ul = ql[E2D_IU], vl = ql[E2D_IV];
+  const double rr = fmax(qr[E2D_ID], ph.smallr);
+  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
+  const double ur = qr[E2D_IU], vr = qr[E2D_IV];
+  double ecinl = 0.5 * rl * ul * ul;
+  ecinl = ecinl + 0.5 * rl * vl * vl;
+  const double etotl = pl * ph.entho + ecinl;
+  double ecinr = 0.5 * rr * ur * ur;
+  ecinr = ecinr + 0.5 * rr * vr * vr;
+  const double etotr = pr * ph.entho + ecinr;
+  const double cfastl = sqrt(fmax(ph.gamma0 * pl / rl, ph.smallc2));
+  const double cfastr = sqrt(fmax(ph.gamma0 * pr / rr, ph.smallc2));
+  const double cmax = fmax(cfastl, cfastr);
+  const double SL = fmin(ul, ur) - cmax;
+  const double SR = fmax(ul, ur) + cmax;
+  const double UL[4] = {rl, etotl, rl * ul, rl * vl};
+  const double UR[4] = {rr, etotr, rr * ur, rr * vr};
+  double FL[4], FR[4];
+  FL[E2D_ID] = UL[E2D_IU];
+  FL[E2D_IP] = (etotl + pl) * ul;
+  FL[E2D_IU] = UL[E2D_IU] * ul + pl;
+  FL[E2D_IV] = UL[E2D_IU] * vl;
+  FR[E2D_ID] = UR[E2D_IU];
+  FR[E2D_IP] = (etotr + pr) * ur;
+  FR[E2D_IU] = UR[E2D_IU] * ur + pr;
+  FR[E2D_IV] = UR[E2D_IU] * vr;
+  if (SL > 0.0) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) flux[v] = FL[v];
+  } else if (SR <= 0.0) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) flux[v] = FR[v];
+  } else {
+    const double sls = SL * SR;
+    const double den = SR - SL;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) / den;
+  }
+}
+
+template <int RS>
+__device__ __forceinline__ void riemann(const KPhys<double> &ph, const double *ql, const double *qr,
+                                        double *flux) {
+  if (RS == E2D_RIEMANN_HLLC)
+    riemann_hllc(ph, ql, qr, flux);
+  else if (RS == E2D_RIEMANN_HLL)
+    riemann_hll(ph, ql, qr, flux);
+  else
+    riemann_approx(ph, ql, qr, flux);
+}
+
+// ------------------------------------------------------------ kernel 1
+// Ghost fill + primitives + CFL maximum (see the file comment).
+__global__ void __launch_bounds__(FILL_BX *FILL_BY)
+    k_fill_f64(const KParams64 kp, double *__restrict__ u_in, double *__restrict__ u_out,
+               double *__restrict__ q, DevClock *clk, const int mode) {
+  if ((mode & FILL_DEVICE_CLOCK) && !(clk->t < clk->t_end)) return;
+  const KGeom &g = kp.g;
+  const KPhys<double> &ph = kp.ph;
+  const int i = blockIdx.x * FILL_BX + threadIdx.x;
+  const int j = blockIdx.y * FILL_BY + threadIdx.y;
+  double term = 0.0;
+  unsigned int flags = 0;
+  if (i < g.isize && j < g.jsize) {
+    bool fu, fv;
+    const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
+    const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
+    const bool ghost = (si != i) || (sj != j);
+    const size_t s = (size_t)si + (size_t)g.isize * sj;
+    const double rho = u_in[s];
+    const double e = u_in[s + g.plane];
+    double mx = u_in[s + 2 * g.plane];
+    double my = u_in[s + 3 * g.plane];
+    if (fu) mx = -mx;
+    if (fv) my = -my;
+    const size_t d = (size_t)i + (size_t)g.isize * j;
+    if (ghost) {
+      if (mode & FILL_GHOSTS_IN) {
+        u_in[d] = rho;
+        u_in[d + g.plane] = e;
+        u_in[d + 2 * g.plane] = mx;
+        u_in[d + 3 * g.plane] = my;
+      }
+      if (mode & FILL_GHOSTS_OUT) {
+        u_out[d] = rho;
+        u_out[d + g.plane] = e;
+        u_out[d + 2 * g.plane] = mx;
+        u_out[d + 3 * g.plane] = my;
+      }
+    }
+    if (mode & (FILL_WRITE_Q | FILL_DT)) {
+      // src/HydroBaseFunctor.h:76-102 (computePrimitives)
+      const double dd = fmax(rho, ph.smallr);
+      const double ux = mx / dd;
+      const double uy = my / dd;
+      const double eken = 0.5 * (ux * ux + uy * uy);
+      const double ei = e / dd - eken;
+      const double p = fmax(ph.gm1 * dd * ei, dd * ph.smallp);
+      if (mode & FILL_WRITE_Q) {
+        q[d] = dd;
+        q[d + g.plane] = p;
+        q[d + 2 * g.plane] = ux;
+        q[d + 3 * g.plane] = uy;
+      }
+      if ((mode & FILL_DT) && !ghost) {
+        // src/HydroRunFunctors.h:56-72
+        const double c = sqrt(ph.gamma0 * p / dd);
+        const double vx = c + fabs(ux);
+        const double vy = c + fabs(uy);
+        term = vx / ph.dx + vy / ph.dy;
+        if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) flags |= E2D_FLAG_NONFINITE;
+        if (!(rho > 0.0)) flags |= E2D_FLAG_DENSITY;
+      }
+    }
+  }
+  if (!(mode & FILL_DT)) return;
+  // block max of the CFL term (fmax drops NaN like the reference's reducer)
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) term = fmax(term, __shfl_xor_sync(0xffffffffu, term, off));
+  flags = __reduce_or_sync(0xffffffffu, flags);
+  __shared__ double wmax[FILL_BX * FILL_BY / 32];
+  __shared__ unsigned int wflags[FILL_BX * FILL_BY / 32];
+  const int tid = threadIdx.y * FILL_BX + threadIdx.x;
+  if ((tid & 31) == 0) {
+    wmax[tid >> 5] = term;
+    wflags[tid >> 5] = flags;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double m = wmax[0];
+    unsigned int f = wflags[0];
+    for (int w = 1; w < FILL_BX * FILL_BY / 32; ++w) {
+      m = fmax(m, wmax[w]);
+      f |= wflags[w];
+    }
+    // positive doubles order like their bit patterns
+    if (m > 0.0) atomicMax(&clk->invdt_bits, (unsigned long long)__double_as_longlong(m));
+    if (f) atomicOr(&clk->status, f);
+  }
+}
+
+// ------------------------------------------------------------ kernel 2
+template <int RS>
+__global__ void __launch_bounds__(NT, 2)
+    k_flux_update_f64(const KParams64 kp, const double *__restrict__ q,
+                      const double *__restrict__ u_in, double *__restrict__ u_out, DevClock *clk,
+                      const int use_clock, const double host_dt, double *__restrict__ dt_trace) {
+  extern __shared__ double smem[];
+  double *sQ = smem;                   // [4][QH][QW]  primitives with halo
+  double *sXm = sQ + 4 * QH * QW;      // [4][TY][XW]  XMIN states, then x-fluxes
+  double *sXp = sXm + 4 * TY * XW;     // [4][TY][XW]  XMAX states
+  double *sYm = sXp + 4 * TY * XW;     // [4][YH][TX]  YMIN states, then y-fluxes
+  double *sYp = sYm + 4 * YH * TX;     // [4][YH][TX]  YMAX states
+
+  const KGeom &g = kp.g;
+  const KPhys<double> &ph = kp.ph;
+  const int tid = threadIdx.x;
+
+  // dt of this step: the caller's, or src/main.cpp:128-134 on the device
+  double dt = host_dt, t = 0.0;
+  if (use_clock) {
+    t = clk->t;
+    const double t_end = clk->t_end;
+    if (!(t < t_end)) return;
+    const double inv_dt = __longlong_as_double((long long)clk->invdt_bits);
+    dt = ph.cfl / inv_dt;
+    if (t + dt > t_end) dt = t_end - t;
+  }
+  const double dtdx = dt / ph.dx;
+  const double dtdy = dt / ph.dy;
+
+  const int i0 = blockIdx.x * TX;  // array column of the tile's first halo cell
+  const int j0 = blockIdx.y * TY;
+
+  // stage 1: primitives of the tile and its 2-cell halo
+  for (int k = tid; k < QH * QW; k += NT) {
+    const int y = k / QW, x = k - y * QW;
+    const int gi = i0 + x, gj = j0 + y;
+    if (gi < g.isize && gj < g.jsize) {
+      const size_t s = (size_t)gi + (size_t)g.isize * gj;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sQ[v * QH * QW + k] = q[s + v * g.plane];
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sQ[v * QH * QW + k] = 1.0;
+    }
+  }
+  __syncthreads();
+
+  // stage 2: slopes, trace sources and face states of the tile cells and of
+  // the 1-cell ring (corners excluded) -- src/HydroBaseFunctor.h:214-291
+  const double st = ph.slope_type;
+  for (int k = tid; k < YH * XW; k += NT) {
+    const int yy = k / XW, xx = k - yy * XW;  // cell (xx-1, yy-1) of the tile
+    const bool xin = (xx >= 1) && (xx <= TX);
+    const bool yin = (yy >= 1) && (yy <= TY);
+    if (!xin && !yin) continue;
+    const int c = (yy + 1) * QW + (xx + 1);
+    double qc[4], dqx[4], dqy[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double *P = sQ + v * QH * QW;
+      qc[v] = P[c];
+      if (st == 0.0) {
+        dqx[v] = 0.0;
+        dqy[v] = 0.0;
+      } else {
+        dqx[v] = slope_1d(st, qc[v], P[c + 1], P[c - 1]);
+        dqy[v] = slope_1d(st, qc[v], P[c + QW], P[c - QW]);
+      }
+    }
+    const double r = qc[E2D_ID], p = qc[E2D_IP], u = qc[E2D_IU], vv = qc[E2D_IV];
+    const double drx = dqx[E2D_ID], dpx = dqx[E2D_IP], dux = dqx[E2D_IU], dvx = dqx[E2D_IV];
+    const double dry = dqy[E2D_ID], dpy = dqy[E2D_IP], duy = dqy[E2D_IU], dvy = dqy[E2D_IV];
+    double s0[4];
+    s0[E2D_ID] = -u * drx - vv * dry - (dux + dvy) * r;
+    s0[E2D_IP] = -u * dpx - vv * dpy - (dux + dvy) * ph.gamma0 * p;
+    s0[E2D_IU] = -u * dux - vv * duy - (dpx) / r;
+    s0[E2D_IV] = -u * dvx - vv * dvy - (dpy) / r;
+    if (yin) {
+      const int o = (yy - 1) * XW + xx;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double h = 0.5 * dqx[v];
+        const double sx = s0[v] * dtdx * 0.5;
+        double fm = qc[v] - h + sx;
+        double fp = qc[v] + h + sx;
+        if (v == E2D_ID) {
+          fm = fmax(ph.smallr, fm);
+          fp = fmax(ph.smallr, fp);
+        }
+        if (xx >= 1) sXm[v * TY * XW + o] = fm;
+        if (xx <= TX) sXp[v * TY * XW + o] = fp;
+      }
+    }
+    if (xin) {
+      const int o = yy * TX + (xx - 1);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double h = 0.5 * dqy[v];
+        const double sy = s0[v] * dtdy * 0.5;
+        double fm = qc[v] - h + sy;
+        double fp = qc[v] + h + sy;
+        if (v == E2D_ID) {
+          fm = fmax(ph.smallr, fm);
+          fp = fmax(ph.smallr, fp);
+        }
+        if (yy >= 1) sYm[v * YH * TX + o] = fm;
+        if (yy <= TY) sYp[v * YH * TX + o] = fp;
+      }
+    }
+  }
+  __syncthreads();
+
+  // stage 3: one Riemann solve per face; the scaled flux replaces the
+  // right-hand state, which no other face reads
+  constexpr int NXF = (TX + 1) * TY;
+  constexpr int NYF = TX * (TY + 1);
+  for (int k = tid; k < NXF + NYF; k += NT) {
+    double ql[4], qr[4], f[4];
+    if (k < NXF) {
+      const int y = k / (TX + 1), fx = k - y * (TX + 1);
+      const int ol = y * XW + fx, orr = ol + 1;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        ql[v] = sXp[v * TY * XW + ol];
+        qr[v] = sXm[v * TY * XW + orr];
+      }
+      riemann<RS>(ph, ql, qr, f);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sXm[v * TY * XW + orr] = f[v] * dtdx;
+    } else {
+      const int kk = k - NXF;
+      const int fy = kk / TX, x = kk - fy * TX;
+      const int ol = fy * TX + x, orr = ol + TX;
+      // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
+        ql[vs] = sYp[v * YH * TX + ol];
+        qr[vs] = sYm[v * YH * TX + orr];
+      }
+      riemann<RS>(ph, ql, qr, f);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
+        sYm[v * YH * TX + orr] = f[vs] * dtdy;
+      }
+    }
+  }
+  __syncthreads();
+
+  // stage 4: conservative update in the reference's order
+  // (src/HydroRunFunctors.h:691-713): +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
+  for (int k = tid; k < TX * TY; k += NT) {
+    const int y = k / TX, x = k - y * TX;
+    const int gi = i0 + 2 + x, gj = j0 + 2 + y;
+    if (gi < g.nx + 2 && gj < g.ny + 2) {
+      const size_t s = (size_t)gi + (size_t)g.isize * gj;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        double uu = u_in[s + v * g.plane];
+        uu = uu + sXm[v * TY * XW + y * XW + x + 1];
+        uu = uu - sXm[v * TY * XW + y * XW + x + 2];
+        uu = uu + sYm[v * YH * TX + (y + 1) * TX + x];
+        uu = uu - sYm[v * YH * TX + (y + 2) * TX + x];
+        u_out[s + v * g.plane] = uu;
+      }
+    }
+  }
+
+  if (!use_clock) return;
+  // the last block to finish advances the loop state (src/main.cpp:139-143)
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned int nblocks = gridDim.x * gridDim.y;
+    const unsigned int ticket = atomicAdd(&clk->done_blocks, 1u);
+    if (ticket == nblocks - 1) {
+      __threadfence();
+      const int ns = clk->nstep;
+      const int slot = ns - clk->trace_base;
+      if (dt_trace && slot >= 0 && slot < clk->trace_cap) dt_trace[slot] = dt;
+      if (!(dt > 0.0) || nonfinite(dt)) clk->status |= E2D_FLAG_BAD_DT;
+      clk->dt = dt;
+      clk->t = t + dt;
+      clk->nstep = ns + 1;
+      clk->invdt_bits = 0ull;
+      clk->done_blocks = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------------ initial conditions
+// src/HydroRunFunctors.h:1347-1827: cell centres x = xmin + dx/2 + (i-g)*dx.
+__global__ void k_init_f64(const KParams64 kp, const e2d_params p, double *__restrict__ u,
+                           const double blast_e_inside) {
+  const KGeom &g = kp.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.isize || j >= g.jsize) return;
+  const double gamma0 = p.gamma0;
+  const double x = p.xmin + p.dx / 2 + (i - 2) * p.dx;
+  const double y = p.ymin + p.dy / 2 + (j - 2) * p.dy;
+  double d = 0, e = 0, mx = 0, my = 0;
+  switch (p.problemType) {
+    case E2D_PROBLEM_IMPLODE: {  // :1375-1401
+      bool in;
+      if (p.implode_shape == 0) {
+        const double tmp = x + y * y;
+        in = tmp > 0.5 && tmp < 1.5;
+      } else {
+        in = x + y > 0.5;
+      }
+      d = in ? 1.0 : 0.125;
+      e = in ? 1.0 / (gamma0 - 1.0) : 0.14 / (gamma0 - 1.0);
+      break;
+    }
+    case E2D_PROBLEM_BLAST: {  // :1451-1520
+      const double r2 = p.blast_radius * p.blast_radius;
+      const double d2 = (x - p.blast_center_x) * (x - p.blast_center_x) +
+                        (y - p.blast_center_y) * (y - p.blast_center_y);
+      const bool in = d2 < r2;
+      d = in ? p.blast_density_in : p.blast_density_out;
+      e = (in ? p.blast_pressure_in : p.blast_pressure_out) / (gamma0 - 1.0);
+      if (in && blast_e_inside > 0.0) e = blast_e_inside;
+      break;
+    }
+    case E2D_PROBLEM_FOUR_QUADRANT: {  // :1578-1665, Lax-Liu case 3
+      const double S[4][4] = {{1.5, 1.5, 0.0, 0.0},
+                              {0.5323, 0.3, 1.206, 0.0},
+                              {0.138, 0.029, 1.206, 1.206},
+                              {0.5323, 0.3, 0.0, 1.206}};
+      const int r = (x < p.fq_split_x) ? ((y < p.fq_split_y) ? 2 : 1) : ((y < p.fq_split_y) ? 3 : 0);
+      const double rho = S[r][0], pr = S[r][1], uu = S[r][2], vv = S[r][3];
+      d = rho;
+      mx = uu * rho;
+      my = vv * rho;
+      e = pr / (gamma0 - 1.0) + rho * (uu * uu + vv * vv) * 0.5;
+      break;
+    }
+    case E2D_PROBLEM_DISCONTINUITY: {  // :1697-1731
+      if (x + y < 1) {
+        d = 1.0 + x * x;
+      } else {
+        d = 0.25;
+      }
+      e = 1.0 / (gamma0 - 1.0);
+      break;
+    }
+    default: {  // E2D_PROBLEM_SHOCKED_BUBBLE, :1761-1822
+      if (x < p.shock_loc) {
+        d = p.postshock_density;
+        mx = p.postshock_density * p.postshock_velocity;
+        my = 0.0;
+        const double rho_eint = p.postshock_pressure / (gamma0 - 1);
+        e = rho_eint + 0.5 * (mx * mx + my * my) / d;
+      } else {
+        const double rad = sqrt((x - p.bubble_center_x) * (x - p.bubble_center_x) +
+                                (y - p.bubble_center_y) * (y - p.bubble_center_y));
+        const bool in = rad < p.bubble_radius;
+        d = in ? p.bubble_density : p.preshock_density;
+        const double rho_eint = (in ? p.bubble_pressure : p.preshock_pressure) / (gamma0 - 1);
+        e = rho_eint + 0.5 * (mx * mx + my * my) / d;
+      }
+      break;
+    }
+  }
+  const size_t o = (size_t)i + (size_t)g.isize * j;
+  u[o] = d;
+  u[o + g.plane] = e;
+  u[o + 2 * g.plane] = mx;
+  u[o + 3 * g.plane] = my;
+}
+
+}  // namespace
+
+size_t flux_update_f64_smem_bytes() { return kSmemDoubles * sizeof(double); }
+
+cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, double *q,
+                            DevClock *clk, int mode, cudaStream_t s) {
+  dim3 block(FILL_BX, FILL_BY);
+  dim3 grid((kp.g.isize + FILL_BX - 1) / FILL_BX, (kp.g.jsize + FILL_BY - 1) / FILL_BY);
+  k_fill_f64<<<grid, block, 0, s>>>(kp, u_in, u_out, q, clk, mode);
+  return cudaGetLastError();
+}
+
+template <int RS>
+static cudaError_t launch_flux_t(const KParams64 &kp, const double *q, const double *u_in,
+                                 double *u_out, DevClock *clk, int use_clock, double host_dt,
+                                 double *dt_trace, cudaStream_t s) {
+  dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
+  k_flux_update_f64<RS><<<grid, NT, flux_update_f64_smem_bytes(), s>>>(kp, q, u_in, u_out, clk,
+                                                                      use_clock, host_dt, dt_trace);
+  return cudaGetLastError();
+}
+
+cudaError_t configure_f64_kernels() {
+  const int smem = (int)flux_update_f64_smem_bytes();
+  cudaError_t e;
+  e = cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_HLLC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_APPROX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const double *q,
+                                   const double *u_in, double *u_out, DevClock *clk,
+                                   int use_clock, double host_dt, double *dt_trace,
+                                   cudaStream_t s) {
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC:
+      return launch_flux_t<E2D_RIEMANN_HLLC>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
+    case E2D_RIEMANN_HLL:
+      return launch_flux_t<E2D_RIEMANN_HLL>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
+    default:
+      return launch_flux_t<E2D_RIEMANN_APPROX>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
+  }
+}
+
+cudaError_t launch_init_f64(const KParams64 &kp, const e2d_params &p, double *u, cudaStream_t s) {
+  // Sedov variant (src/HydroRunFunctors.h:1425-1447, :1496-1547): the
+  // inside energy is total_energy_inside / (inside cell count * dx * dy).
+  double e_inside = 0.0;
+  if (p.problemType == E2D_PROBLEM_BLAST && p.blast_total_energy_inside > 0) {
+    long long count = 0;
+    const double r2 = p.blast_radius * p.blast_radius;
+    for (int j = 0; j < kp.g.jsize; ++j)
+      for (int i = 0; i < kp.g.isize; ++i) {
+        const double x = p.xmin + p.dx / 2 + (i - 2) * p.dx;
+        const double y = p.ymin + p.dy / 2 + (j - 2) * p.dy;
+        const double d2 = (x - p.blast_center_x) * (x - p.blast_center_x) +
+                          (y - p.blast_center_y) * (y - p.blast_center_y);
+        if (d2 < r2) count++;
+      }
+    if (count > 0) e_inside = p.blast_total_energy_inside / ((double)count * (p.dx * p.dy));
+  }
+  dim3 block(64, 4);
+  dim3 grid((kp.g.isize + 63) / 64, (kp.g.jsize + 3) / 4);
+  k_init_f64<<<grid, block, 0, s>>>(kp, p, u, e_inside);
+  return cudaGetLastError();
+}
+
+}  // namespace e2d

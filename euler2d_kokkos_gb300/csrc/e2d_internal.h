@@ -1,0 +1,102 @@
+// e2d_internal.h -- shared declarations of the GB300 euler2d library:
+// the ini reader, the parameter helpers, the device-side parameter blocks,
+// the device clock and the kernel launchers of each arithmetic mode.
+#pragma once
+
+#include <map>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/e2d.h"
+
+namespace e2d {
+
+// ---------------------------------------------------------------- host side
+class IniMap {
+ public:
+  // 0 on success, -1 if the file cannot be opened, else the first bad line.
+  int parse(const char *path);
+  std::string get_string(const std::string &section, const std::string &name,
+                         const std::string &dflt) const;
+  long get_integer(const std::string &section, const std::string &name, long dflt) const;
+  float get_float(const std::string &section, const std::string &name, float dflt) const;
+  bool get_bool(const std::string &section, const std::string &name, bool dflt) const;
+
+ private:
+  std::map<std::string, std::string> values_;
+};
+
+void params_defaults(e2d_params *p);
+int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg);
+int params_init(e2d_params *p, std::string *msg);
+
+// ---------------------------------------------------------------- device side
+// Grid geometry as every kernel sees it.
+struct KGeom {
+  int nx, ny, isize, jsize;
+  long long plane;  // isize * jsize: stride between the 4 variable planes
+  int bc_xmin, bc_xmax, bc_ymin, bc_ymax;
+};
+
+// Physics constants in the step's arithmetic type.  gm1, entho and smallc2
+// are computed on the host with the same operations the reference performs
+// inline (gamma0 - 1.0, 1.0 / (gamma0 - 1.0), smallc * smallc), so using them
+// changes no bit of the result.
+template <typename R>
+struct KPhys {
+  R gamma0, gamma6, cfl, slope_type, smallr, smallc, smallp, smallpp;
+  R gm1, entho, smallc2;
+  R dx, dy;
+};
+
+struct KParams64 {
+  KGeom g;
+  KPhys<double> ph;
+};
+
+// Device-resident loop state of the time loop of src/main.cpp:100-145.
+struct DevClock {
+  double t;                       // simulated time
+  double t_end;                   // loop ends once t >= t_end
+  double dt;                      // dt of the last step taken
+  unsigned long long invdt_bits;  // running max of the CFL wave-speed term (bits of a double >= 0)
+  int nstep;                      // steps taken since the start of the run
+  int trace_base;                 // nstep of the first entry of the dt trace buffer
+  int trace_cap;                  // entries available in the dt trace buffer
+  unsigned int done_blocks;       // blocks of the current step kernel that finished
+  unsigned int status;            // E2D_FLAG_* bits seen by the device
+  unsigned int fill_count;        // blocks of the current primitives kernel that finished
+};
+
+enum : unsigned int {
+  E2D_FLAG_NONFINITE = 1u,  // a state value is NaN or Inf
+  E2D_FLAG_DENSITY = 2u,    // a density <= 0 was clamped to smallr
+  E2D_FLAG_BAD_DT = 4u,     // the CFL wave-speed maximum is not a finite positive number
+};
+
+// Modes of the primitives kernel.
+enum : int {
+  FILL_WRITE_Q = 1,          // store primitives of every cell
+  FILL_GHOSTS_IN = 2,        // store the ghost fill into the input state (make_boundaries)
+  FILL_GHOSTS_OUT = 4,       // store the ghost fill into the output state (deep_copy)
+  FILL_DT = 8,               // fold the CFL term of interior cells into clock->invdt_bits
+  FILL_DEVICE_CLOCK = 16,    // do nothing once clock->t >= clock->t_end
+};
+
+// FP64 kernels (e2d_fp64.cu, bit-identical to the reference).
+cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, double *q,
+                            DevClock *clk, int mode, cudaStream_t s);
+// use_clock = 1: dt from clk (src/main.cpp:128-134 on the device) and the
+// loop bookkeeping; 0: the caller's host_dt, clock untouched.
+cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const double *q,
+                                   const double *u_in, double *u_out, DevClock *clk,
+                                   int use_clock, double host_dt, double *dt_trace,
+                                   cudaStream_t s);
+// Sets the kernels' shared-memory limits; call once per device before any
+// launch or graph capture.
+cudaError_t configure_f64_kernels();
+cudaError_t launch_init_f64(const KParams64 &kp, const e2d_params &p, double *u, cudaStream_t s);
+size_t flux_update_f64_smem_bytes();
+
+}  // namespace e2d

@@ -1,0 +1,167 @@
+/*
+ * e2d.h -- C ABI of the GB300-native unsplit MUSCL-Hancock Godunov step.
+ *
+ * Drop-in for the hot path of euler2d_kokkos: the class template
+ * euler2d::HydroRun<device_t> (src/HydroRun.h:44-134) with its
+ * compute_dt / godunov_unsplit / make_boundaries methods, the HydroParams
+ * parameter contract (src/HydroParams.h:107-265) and the ConfigMap ini reader
+ * (config/ConfigMap.h:25-47).  The reference has no FFI: these entry points
+ * are what a C, ctypes, cgo or JNI binding of that class would call.  Each
+ * declaration names the reference interface it replaces.
+ *
+ * Conventions
+ *  - Every function returns an e2d_status (0 = E2D_OK).  Failures never abort
+ *    the process; e2d_last_error() gives the message of the last failure on a
+ *    handle.
+ *  - Device memory is owned by the handle.  Host buffers belong to the caller.
+ *  - A handle is used from one host thread; its work runs on its own CUDA
+ *    stream (e2d_get_stream).
+ *  - State arrays hold (rho, E, rho*u, rho*v) for isize*jsize cells, ghosts
+ *    included, in the reference's DataArray layout on its CUDA backend
+ *    (LayoutLeft: element (i, j, v) at i + isize*(j + jsize*v)).  Host copies
+ *    may also use the OpenMP backend's LayoutRight ((i*jsize + j)*4 + v).
+ */
+#ifndef E2D_H_
+#define E2D_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define E2D_ABI_VERSION 1
+
+typedef enum e2d_status {
+  E2D_OK = 0,
+  E2D_EINVAL = 1,   /* bad argument or parameter                        */
+  E2D_ENOMEM = 2,   /* device or host allocation failed                 */
+  E2D_ENUMERIC = 3, /* device saw NaN/Inf, rho <= 0, p <= 0 or dt <= 0  */
+  E2D_ETIMEOUT = 4, /* a bounded device wait gave up                    */
+  E2D_ECUDA = 5,    /* a CUDA runtime call failed                       */
+  E2D_EIO = 6       /* ini file missing or unreadable                   */
+} e2d_status;
+
+/* Values of src/HydroParams.h:26-102 (ComponentIndex, RiemannSolverType,
+ * BoundaryConditionType, ProblemType). */
+enum { E2D_ID = 0, E2D_IP = 1, E2D_IE = 1, E2D_IU = 2, E2D_IV = 3 };
+enum { E2D_RIEMANN_APPROX = 0, E2D_RIEMANN_HLL = 1, E2D_RIEMANN_HLLC = 2 };
+enum { E2D_BC_REFLECT = 1, E2D_BC_ABSORB = 2, E2D_BC_PERIODIC = 3 };
+enum {
+  E2D_PROBLEM_IMPLODE = 0,
+  E2D_PROBLEM_BLAST = 1,
+  E2D_PROBLEM_FOUR_QUADRANT = 2,
+  E2D_PROBLEM_DISCONTINUITY = 3,
+  E2D_PROBLEM_SHOCKED_BUBBLE = 4
+};
+enum { E2D_LAYOUT_LEFT = 0, E2D_LAYOUT_RIGHT = 1 };
+/* Arithmetic of the step: FP64 (bit-identical to the reference) or FP32
+ * with a compensated hi/lo conservative update. */
+enum { E2D_PRECISION_FP64 = 0, E2D_PRECISION_FP32C = 1 };
+
+/* Flat mirror of HydroParams + HydroSettings (src/HydroParams.h:107-265).
+ * Fill it with e2d_params_from_ini (the reference's ini semantics, reals
+ * rounded to float as ConfigMap::getFloat does) or e2d_params_defaults, then
+ * call e2d_params_init for the derived members. */
+typedef struct e2d_params {
+  /* [run] */
+  int nStepmax;
+  double tEnd;
+  int nOutput;
+  /* [mesh] */
+  int nx, ny, ghostWidth;
+  double xmin, xmax, ymin, ymax;
+  int boundary_type_xmin, boundary_type_xmax, boundary_type_ymin, boundary_type_ymax;
+  /* [hydro] */
+  double gamma0, cfl, slope_type, smallr, smallc;
+  int niter_riemann;
+  int riemannSolverType;
+  int problemType;
+  /* [blast] */
+  double blast_radius, blast_center_x, blast_center_y;
+  double blast_density_in, blast_density_out, blast_pressure_in, blast_pressure_out;
+  double blast_total_energy_inside;
+  /* [shocked_bubble] */
+  double bubble_radius, bubble_center_x, bubble_center_y, bubble_density, bubble_pressure;
+  double preshock_density, preshock_pressure, postshock_density, postshock_pressure;
+  double postshock_velocity, shock_loc;
+  /* [four_quadrant] split point (the reference hard-codes 0.8, 0.8) */
+  double fq_split_x, fq_split_y;
+  /* [implode] shape: 0 = the reference's x + y*y in (0.5, 1.5) band,
+   * 1 = the classic diagonal split x + y > 0.5 */
+  int implode_shape;
+  /* [OTHER] implementationVersion: 0, 1 or 2 all run the fused step */
+  int implementationVersion;
+  /* GB300 build: arithmetic mode */
+  int precision;
+  /* derived by e2d_params_init (HydroParams::init, src/HydroParams.cpp:160-190) */
+  int imin, imax, jmin, jmax, isize, jsize;
+  double dx, dy, smallp, smallpp, gamma6;
+} e2d_params;
+
+typedef struct e2d_sim e2d_sim;
+
+/* ABI version compiled into the library (E2D_ABI_VERSION). */
+int e2d_abi_version(void);
+/* Human-readable name of a status code. */
+const char *e2d_status_string(int status);
+
+/* Defaults of HydroParams::setup (src/HydroParams.cpp:42-156). */
+int e2d_params_defaults(e2d_params *p);
+/* ConfigMap(path) + HydroParams::setup (config/ConfigMap.cpp:21-40,
+ * src/HydroParams.cpp:42-156): case-insensitive keys, reals via strtof. */
+int e2d_params_from_ini(const char *path, e2d_params *p);
+/* HydroParams::init (src/HydroParams.cpp:160-190); validates the values. */
+int e2d_params_init(e2d_params *p);
+
+/* HydroRun<device>::HydroRun (src/HydroRun.h:143-216) without the initial
+ * condition: allocates U and U2 on the device (zeroed). */
+int e2d_create(const e2d_params *p, e2d_sim **out);
+/* ~HydroRun: frees every device buffer of the handle. */
+int e2d_destroy(e2d_sim *sim);
+/* Last failure message on this handle ("" if none). */
+const char *e2d_last_error(const e2d_sim *sim);
+/* The copy of the parameters the handle runs with. */
+int e2d_get_params(const e2d_sim *sim, e2d_params *p);
+
+/* The initial condition of HydroRun's constructor (src/HydroRun.h:185-214,
+ * InitXxxFunctor in src/HydroRunFunctors.h:1347-1827) into U, then U2 = U. */
+int e2d_init_problem(e2d_sim *sim);
+/* Host -> device copy of a whole state (which = 0: U, 1: U2). */
+int e2d_set_state(e2d_sim *sim, int which, const double *host, int layout);
+/* Device -> host copy of a whole state (which = 0: U, 1: U2); synchronises. */
+int e2d_get_state(e2d_sim *sim, int which, double *host, int layout);
+/* Device address of U (which = 0) or U2 (1), LayoutLeft, for zero-copy use. */
+int e2d_device_state(e2d_sim *sim, int which, double **dptr);
+/* The handle's CUDA stream (a cudaStream_t). */
+int e2d_get_stream(e2d_sim *sim, void **stream);
+
+/* HydroRun::make_boundaries (src/HydroRun.h:388-399) on U (0) or U2 (1). */
+int e2d_make_boundaries(e2d_sim *sim, int which);
+/* HydroRun::compute_dt (src/HydroRun.h:227-251): cfl / max wave speed of U
+ * (useU == 0) or U2; blocks until the value is on the host. */
+int e2d_compute_dt(e2d_sim *sim, int useU, double *dt);
+/* HydroRun::godunov_unsplit (src/HydroRun.h:258-272): U -> U2 for even
+ * nStep, U2 -> U for odd, with the caller's dt.  Asynchronous. */
+int e2d_godunov_unsplit(e2d_sim *sim, int nStep, double dt);
+
+/* The time loop of src/main.cpp:100-145 for up to n steps on the device:
+ * each step takes dt = cfl/max wave speed of the current state, clamps it to
+ * t_end - t, runs godunov_unsplit and advances (t, nStep); steps with
+ * t >= t_end do nothing.  *t and *nStep are read and updated.  dt_trace
+ * (optional, n entries) receives the dt of each step taken.  Launches are
+ * replayed from cached CUDA graphs.  Blocks until done. */
+int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double *dt_trace);
+
+/* Per-kernel device time: with profiling on, e2d_step_n launches kernels
+ * directly with CUDA events around each one.  names/ms/launches receive, per
+ * kernel, its name, total milliseconds and launch count. */
+int e2d_set_profiling(e2d_sim *sim, int on);
+int e2d_kernel_times(e2d_sim *sim, int max_kernels, const char **names, double *ms, long *launches,
+                     int *n_kernels);
+int e2d_reset_kernel_times(e2d_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* E2D_H_ */
