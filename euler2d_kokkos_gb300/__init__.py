@@ -52,6 +52,7 @@ class _Params(ctypes.Structure):
     # field order of struct e2d_params (include/e2d.h)
     _fields_ = [
         ("nStepmax", ctypes.c_int), ("tEnd", ctypes.c_double), ("nOutput", ctypes.c_int),
+        ("enableOutput", ctypes.c_int), ("ioVTK", ctypes.c_int), ("ioHDF5", ctypes.c_int),
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("ghostWidth", ctypes.c_int),
         ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
         ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
@@ -65,6 +66,7 @@ class _Params(ctypes.Structure):
         ("blast_center_y", ctypes.c_double), ("blast_density_in", ctypes.c_double),
         ("blast_density_out", ctypes.c_double), ("blast_pressure_in", ctypes.c_double),
         ("blast_pressure_out", ctypes.c_double), ("blast_total_energy_inside", ctypes.c_double),
+        ("blast_nbins", ctypes.c_int),
         ("bubble_radius", ctypes.c_double), ("bubble_center_x", ctypes.c_double),
         ("bubble_center_y", ctypes.c_double), ("bubble_density", ctypes.c_double),
         ("bubble_pressure", ctypes.c_double), ("preshock_density", ctypes.c_double),
@@ -93,6 +95,9 @@ SIGNATURES = {
     "e2d_params_defaults": ([_P], _I),
     "e2d_params_from_ini": ([ctypes.c_char_p, _P], _I),
     "e2d_params_init": ([_P], _I),
+    "e2d_ini_get_string": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                            ctypes.c_char_p, ctypes.c_size_t], _I),
+    "e2d_save_vtk": ([_V, _I, ctypes.c_char_p], _I),
     "e2d_create": ([_P, ctypes.POINTER(_V)], _I),
     "e2d_destroy": ([_V], _I),
     "e2d_last_error": ([_V], ctypes.c_char_p),

@@ -190,6 +190,18 @@ int e2d_params_init(e2d_params *p) {
   return params_init(p, nullptr);
 }
 
+int e2d_ini_get_string(const char *path, const char *section, const char *name, const char *dflt,
+                       char *buf, size_t buflen) {
+  if (!path || !section || !name || !buf || buflen == 0) return E2D_EINVAL;
+  IniMap m;
+  if (m.parse(path) < 0) return E2D_EIO;
+  const std::string v = m.get_string(section, name, dflt ? dflt : "");
+  const size_t n = v.size() < buflen - 1 ? v.size() : buflen - 1;
+  std::memcpy(buf, v.data(), n);
+  buf[n] = '\0';
+  return E2D_OK;
+}
+
 int e2d_create(const e2d_params *pin, e2d_sim **out) {
   if (!pin || !out) return E2D_EINVAL;
   *out = nullptr;
@@ -302,6 +314,40 @@ int e2d_get_state(e2d_sim *s, int which, double *host, int layout) {
     left_to_right(s->p, tmp.data(), host);
   }
   return E2D_OK;
+}
+
+int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
+  if (!s || !filename || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad save_vtk args");
+  const e2d_params &p = s->p;
+  std::vector<double> host(state_count(s));
+  int rc = e2d_get_state(s, which, host.data(), E2D_LAYOUT_LEFT);
+  if (rc != E2D_OK) return rc;
+  FILE *f = std::fopen(filename, "w");
+  if (!f) return set_err(s, E2D_EIO, std::string("cannot open ") + filename);
+  // text layout of src/HydroRun.h:557-607; numbers in the default ostream
+  // format (%g, 6 significant digits)
+  static const char *names[4] = {"rho", "E", "mx", "my"};
+  const int one = 1;
+  const bool big = (*(const char *)&one) == 0;
+  std::fprintf(f, "<?xml version=\"1.0\"?>\n");
+  std::fprintf(f, "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"%s\">\n",
+               big ? "BigEndian" : "LittleEndian");
+  std::fprintf(f, "  <ImageData WholeExtent=\"0 %d 0 %d 0 0\" Origin=\"%g %g 0\" Spacing=\"%g %g 0\">\n",
+               p.nx, p.ny, p.xmin, p.ymin, p.dx, p.dy);
+  std::fprintf(f, "  <Piece Extent=\"0 %d 0 %d 0 0 \">\n", p.nx, p.ny);
+  std::fprintf(f, "    <PointData>\n    </PointData>\n    <CellData>\n");
+  const size_t plane = (size_t)p.isize * p.jsize;
+  for (int v = 0; v < 4; ++v) {
+    std::fprintf(f, "    <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\" >\n", names[v]);
+    for (int j = 2; j <= p.jsize - 3; ++j)
+      for (int i = 2; i <= p.isize - 3; ++i)
+        std::fprintf(f, "%g ", host[i + (size_t)p.isize * j + plane * v]);
+    std::fprintf(f, "\n    </DataArray>\n");
+  }
+  std::fprintf(f, "    </CellData>\n  </Piece>\n  </ImageData>\n</VTKFile>\n");
+  const bool ok = std::ferror(f) == 0;
+  std::fclose(f);
+  return ok ? E2D_OK : set_err(s, E2D_EIO, std::string("write failed: ") + filename);
 }
 
 int e2d_make_boundaries(e2d_sim *s, int which) {

@@ -145,6 +145,10 @@ void params_defaults(e2d_params *p) {
   p->nStepmax = 1000;
   p->tEnd = 0.0;
   p->nOutput = 100;
+  p->enableOutput = 1;
+  p->ioVTK = 1;
+  p->ioHDF5 = 0;
+  p->blast_nbins = 100;
   p->nx = 2;
   p->ny = 2;
   p->ghostWidth = 2;
@@ -194,6 +198,10 @@ int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
   p->nStepmax = (int)m.get_integer("run", "nstepmax", 1000);
   p->tEnd = m.get_float("run", "tend", 0.0f);
   p->nOutput = (int)m.get_integer("run", "noutput", 100);
+  p->enableOutput = (p->nOutput == -1) ? 0 : 1;
+  // the defaults of a build without HDF5 (src/HydroParams.cpp:54-60)
+  p->ioHDF5 = m.get_bool("run", "use_HDF5", false) ? 1 : 0;
+  p->ioVTK = m.get_bool("run", "use_VTK", true) ? 1 : 0;
 
   p->nx = (int)m.get_integer("mesh", "nx", 2);
   p->ny = (int)m.get_integer("mesh", "ny", 2);
@@ -264,6 +272,7 @@ int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
   p->blast_pressure_in = m.get_float("blast", "pressure_in", 10.0f);
   p->blast_pressure_out = m.get_float("blast", "pressure_out", 0.1f);
   p->blast_total_energy_inside = m.get_float("blast", "total_energy_inside", 0.0f);
+  p->blast_nbins = (int)m.get_integer("blast", "nbins", 100);
 
   // extensions of this build (absent keys keep the reference's behaviour)
   p->fq_split_x = m.get_float("four_quadrant", "split_x", 0.8f);

@@ -68,6 +68,8 @@ typedef struct e2d_params {
   int nStepmax;
   double tEnd;
   int nOutput;
+  int enableOutput; /* 0 when nOutput == -1 */
+  int ioVTK, ioHDF5;
   /* [mesh] */
   int nx, ny, ghostWidth;
   double xmin, xmax, ymin, ymax;
@@ -81,6 +83,7 @@ typedef struct e2d_params {
   double blast_radius, blast_center_x, blast_center_y;
   double blast_density_in, blast_density_out, blast_pressure_in, blast_pressure_out;
   double blast_total_energy_inside;
+  int blast_nbins;
   /* [shocked_bubble] */
   double bubble_radius, bubble_center_x, bubble_center_y, bubble_density, bubble_pressure;
   double preshock_density, preshock_pressure, postshock_density, postshock_pressure;
@@ -113,6 +116,11 @@ int e2d_params_defaults(e2d_params *p);
 int e2d_params_from_ini(const char *path, e2d_params *p);
 /* HydroParams::init (src/HydroParams.cpp:160-190); validates the values. */
 int e2d_params_init(e2d_params *p);
+/* ConfigMap::getString (config/inih/INIReader.cpp:36-42) on an ini file:
+ * the value of section.name (case-insensitive) or dflt, copied with a
+ * terminating NUL into buf (truncated to buflen - 1 bytes). */
+int e2d_ini_get_string(const char *path, const char *section, const char *name, const char *dflt,
+                       char *buf, size_t buflen);
 
 /* HydroRun<device>::HydroRun (src/HydroRun.h:143-216) without the initial
  * condition: allocates U and U2 on the device (zeroed). */
@@ -131,6 +139,10 @@ int e2d_init_problem(e2d_sim *sim);
 int e2d_set_state(e2d_sim *sim, int which, const double *host, int layout);
 /* Device -> host copy of a whole state (which = 0: U, 1: U2); synchronises. */
 int e2d_get_state(e2d_sim *sim, int which, double *host, int layout);
+/* HydroRun::saveVTK (src/HydroRun.h:506-609): device -> host copy of U (0)
+ * or U2 (1) and an ASCII VTK ImageData (.vti) file of the interior cells,
+ * variables rho, E, mx, my in the reference's text format. */
+int e2d_save_vtk(e2d_sim *sim, int which, const char *filename);
 /* Device address of U (which = 0) or U2 (1), LayoutLeft, for zero-copy use. */
 int e2d_device_state(e2d_sim *sim, int which, double **dptr);
 /* The handle's CUDA stream (a cudaStream_t). */

@@ -1,0 +1,158 @@
+// euler2d_gb300.hpp -- C++ host interface of the GB300 euler2d step,
+// header-only over the C ABI of e2d.h.
+//
+// It keeps the names and argument meaning of the reference's driver API so a
+// user of euler2d_kokkos can switch by changing the include and namespace:
+//   ConfigMap         config/ConfigMap.h:25-47 (constructed from an ini path)
+//   HydroParams       src/HydroParams.h:155-265 (setup / init / print)
+//   HydroRun          src/HydroRun.h:44-134 (compute_dt / godunov_unsplit /
+//                     make_boundaries, public U / U2 / Uhost)
+// Differences: errors throw euler2d_gb300::Error instead of exit()/silent
+// fallbacks; DataArray is a device view of one of the handle's two states.
+#pragma once
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "e2d.h"
+
+namespace euler2d_gb300 {
+
+using real_t = double;
+
+class Error : public std::runtime_error {
+ public:
+  Error(int status, const std::string &what)
+      : std::runtime_error(what + ": " + e2d_status_string(status)), status_(status) {}
+  int status() const { return status_; }
+
+ private:
+  int status_;
+};
+
+inline void check(int status, const char *what, const e2d_sim *sim = nullptr) {
+  if (status != E2D_OK) {
+    std::string w(what);
+    if (sim) w += std::string(" (") + e2d_last_error(sim) + ")";
+    throw Error(status, w);
+  }
+}
+
+// ConfigMap: holds the ini path; values are read by HydroParams::setup with
+// the reference's ConfigMap semantics (strtof reals, case-insensitive keys).
+class ConfigMap {
+ public:
+  explicit ConfigMap(std::string filename) : filename_(std::move(filename)) {}
+  const std::string &filename() const { return filename_; }
+
+ private:
+  std::string filename_;
+};
+
+struct HydroParams : public e2d_params {
+  HydroParams() { e2d_params_defaults(this); }
+  void setup(ConfigMap &map) { check(e2d_params_from_ini(map.filename().c_str(), this), "HydroParams::setup"); }
+  void init() { check(e2d_params_init(this), "HydroParams::init"); }
+  void print() const {
+    std::printf("##########################\n");
+    std::printf("Simulation run parameters:\n");
+    std::printf("##########################\n");
+    std::printf("nx         : %d\n", nx);
+    std::printf("ny         : %d\n", ny);
+    std::printf("dx         : %f\n", dx);
+    std::printf("dy         : %f\n", dy);
+    std::printf("imin       : %d\n", imin);
+    std::printf("imax       : %d\n", imax);
+    std::printf("jmin       : %d\n", jmin);
+    std::printf("jmax       : %d\n", jmax);
+    std::printf("nStepmax   : %d\n", nStepmax);
+    std::printf("tEnd       : %f\n", tEnd);
+    std::printf("nOutput    : %d\n", nOutput);
+    std::printf("gamma0     : %f\n", gamma0);
+    std::printf("cfl        : %f\n", cfl);
+    std::printf("smallr     : %12.10f\n", smallr);
+    std::printf("smallc     : %12.10f\n", smallc);
+    std::printf("slope_type : %f\n", slope_type);
+    std::printf("riemann    : %d\n", riemannSolverType);
+    std::printf("problem    : %d\n", problemType);
+    std::printf("implementation version : %d\n", implementationVersion);
+    std::printf("precision  : %s\n", precision == E2D_PRECISION_FP64 ? "fp64" : "fp32c");
+    std::printf("##########################\n");
+  }
+};
+
+// Device view of one state of a HydroRun (LayoutLeft, 4 planes).
+struct DataArray {
+  double *data = nullptr;
+  int isize = 0, jsize = 0;
+  int which = 0;  // 0: U, 1: U2
+  size_t size() const { return (size_t)4 * isize * jsize; }
+};
+
+class HydroRun {
+ public:
+  // src/HydroRun.h:143-216: allocate the states and set the initial condition.
+  HydroRun(HydroParams &params, ConfigMap &configMap) : params(params), configMap(configMap) {
+    check(e2d_create(&params, &sim_), "HydroRun");
+    check(e2d_get_params(sim_, &params), "HydroRun");
+    check(e2d_init_problem(sim_), "HydroRun init", sim_);
+    U = view(0);
+    U2 = view(1);
+  }
+  HydroRun(const HydroRun &) = delete;
+  HydroRun &operator=(const HydroRun &) = delete;
+  virtual ~HydroRun() {
+    if (sim_) e2d_destroy(sim_);
+  }
+
+  HydroParams &params;
+  ConfigMap &configMap;
+  DataArray U, U2;
+  std::vector<double> Uhost;  // host mirror filled by copy_to_host
+
+  // src/HydroRun.h:227-251
+  real_t compute_dt(int useU) {
+    double dt = 0;
+    check(e2d_compute_dt(sim_, useU, &dt), "compute_dt", sim_);
+    return dt;
+  }
+  // src/HydroRun.h:258-272
+  void godunov_unsplit(int nStep, real_t dt) {
+    check(e2d_godunov_unsplit(sim_, nStep, dt), "godunov_unsplit", sim_);
+  }
+  // src/HydroRun.h:388-399
+  void make_boundaries(const DataArray &Udata) {
+    check(e2d_make_boundaries(sim_, Udata.which), "make_boundaries", sim_);
+  }
+  // the time loop of src/main.cpp:100-145 on the device, n steps at most
+  int step_n(int n, real_t tEnd, real_t &t, int &nStep, double *dt_trace = nullptr) {
+    const int before = nStep;
+    check(e2d_step_n(sim_, n, tEnd, &t, &nStep, dt_trace), "step_n", sim_);
+    return nStep - before;
+  }
+  // deep_copy(Uhost, Udata) of src/HydroRun.h:522
+  const std::vector<double> &copy_to_host(const DataArray &Udata) {
+    Uhost.resize(Udata.size());
+    check(e2d_get_state(sim_, Udata.which, Uhost.data(), E2D_LAYOUT_LEFT), "copy_to_host", sim_);
+    return Uhost;
+  }
+  void copy_from_host(const DataArray &Udata, const std::vector<double> &host) {
+    check(e2d_set_state(sim_, Udata.which, host.data(), E2D_LAYOUT_LEFT), "copy_from_host", sim_);
+  }
+  e2d_sim *sim() { return sim_; }
+
+ private:
+  DataArray view(int which) {
+    DataArray d;
+    check(e2d_device_state(sim_, which, &d.data), "device_state");
+    d.isize = params.isize;
+    d.jsize = params.jsize;
+    d.which = which;
+    return d;
+  }
+  e2d_sim *sim_ = nullptr;
+};
+
+}  // namespace euler2d_gb300
