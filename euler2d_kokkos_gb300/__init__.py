@@ -111,6 +111,7 @@ SIGNATURES = {
     "e2d_compute_dt": ([_V, _I, ctypes.POINTER(_D)], _I),
     "e2d_godunov_unsplit": ([_V, _I, _D], _I),
     "e2d_step_n": ([_V, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I), _V], _I),
+    "e2d_eval_device": ([_P, _I, _I, _V, _V, _D, _D], _I),
     "e2d_set_profiling": ([_V, _I], _I),
     "e2d_kernel_times": ([_V, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D),
                           ctypes.POINTER(ctypes.c_long), ctypes.POINTER(_I)], _I),
@@ -329,3 +330,20 @@ class HydroRun:
 
     def reset_kernel_times(self):
         self._lib.e2d_reset_kernel_times(self._h)
+
+
+EVAL = {"primitives": (0, 4, 5), "slopes": (1, 20, 8), "trace_xmin": (2, 12, 4), "trace_xmax": (3, 12, 4),
+        "trace_ymin": (4, 12, 4), "trace_ymax": (5, 12, 4), "riemann_approx": (6, 8, 4),
+        "riemann_hll": (7, 8, 4), "riemann_hllc": (8, 8, 4)}
+
+
+def eval_device(params: HydroParams, what: str, inputs: np.ndarray, dtdx: float = 0.0,
+                dtdy: float = 0.0) -> np.ndarray:
+    """One building block of the FP64 step (e2d_eval_device) on the device,
+    for every row of `inputs` (see include/e2d.h for the row layouts)."""
+    code, w_in, w_out = EVAL[what]
+    x = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, w_in)
+    out = np.zeros((len(x), w_out))
+    _check(load_library().e2d_eval_device(ctypes.byref(params._raw), code, len(x), x.ctypes.data,
+                                          out.ctypes.data, float(dtdx), float(dtdy)), f"eval_device({what})")
+    return out

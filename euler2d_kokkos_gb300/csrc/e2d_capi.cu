@@ -54,7 +54,9 @@ int cuda_fail(e2d_sim *s, cudaError_t e, const char *what) {
     if (e__ != cudaSuccess) return cuda_fail(sim, e__, what); \
   } while (0)
 
-void make_kparams(const e2d_params &p, KParams64 *kp) {
+}  // namespace
+
+void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->g.nx = p.nx;
   kp->g.ny = p.ny;
   kp->g.isize = p.isize;
@@ -78,6 +80,8 @@ void make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->ph.dx = p.dx;
   kp->ph.dy = p.dy;
 }
+
+namespace {
 
 size_t state_count(const e2d_sim *s) { return (size_t)4 * s->p.isize * s->p.jsize; }
 
@@ -450,6 +454,38 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
     return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
                                                                               : "non-positive or non-finite dt");
   return E2D_OK;
+}
+
+int e2d_eval_device(const e2d_params *pin, int what, int n, const double *in, double *out,
+                    double dtdx, double dtdy) {
+  if (!pin || !in || !out || n < 0 || what < E2D_EVAL_PRIMITIVES || what > E2D_EVAL_RIEMANN_HLLC)
+    return E2D_EINVAL;
+  if (n == 0) return E2D_OK;
+  e2d_params p = *pin;
+  const int rc = params_init(&p, nullptr);
+  if (rc != E2D_OK) return rc;
+  KParams64 kp;
+  make_kparams(p, &kp);
+  const int in_w = what == E2D_EVAL_PRIMITIVES ? 4 : what == E2D_EVAL_SLOPES ? 20
+                   : what <= E2D_EVAL_TRACE_YMAX ? 12 : 8;
+  const int out_w = what == E2D_EVAL_PRIMITIVES ? 5 : what == E2D_EVAL_SLOPES ? 8 : 4;
+  double *din = nullptr, *dout = nullptr;
+  cudaStream_t st = nullptr;
+  int status = E2D_OK;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return E2D_ECUDA;
+  if (cudaMalloc(&din, sizeof(double) * in_w * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&dout, sizeof(double) * out_w * (size_t)n) != cudaSuccess) {
+    status = E2D_ENOMEM;
+  } else if (cudaMemcpyAsync(din, in, sizeof(double) * in_w * (size_t)n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+             launch_eval_f64(kp, what, n, din, dout, dtdx, dtdy, st) != cudaSuccess ||
+             cudaMemcpyAsync(out, dout, sizeof(double) * out_w * (size_t)n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+             cudaStreamSynchronize(st) != cudaSuccess) {
+    status = E2D_ECUDA;
+  }
+  if (din) cudaFree(din);
+  if (dout) cudaFree(dout);
+  cudaStreamDestroy(st);
+  return status;
 }
 
 int e2d_set_profiling(e2d_sim *s, int on) {

@@ -16,12 +16,21 @@
 //                      bookkeeping of src/main.cpp:128-143.
 // The reference evaluates the slopes of a cell three times and the trace
 // sources four times per cell; evaluating each once gives the same bits.
+#include "e2d_common.cuh"
+#include "e2d_f64_exact.cuh"
 #include "e2d_internal.h"
 
 #include <cstdint>
 
 namespace e2d {
 namespace {
+
+using f64x::gt0;
+using f64x::half;
+using f64x::max_nn;
+using f64x::max_pos;
+using f64x::max_any;
+using f64x::min_any;
 
 constexpr int TX = 32;        // interior cells per tile along x
 constexpr int TY = 16;        // interior cells per tile along y
@@ -34,47 +43,55 @@ constexpr int FILL_BX = 64, FILL_BY = 4;
 
 constexpr size_t kSmemDoubles = 4 * QH * QW + 2 * (4 * TY * XW) + 2 * (4 * YH * TX);
 
-// ------------------------------------------------------------ ghost map
-// Source cell of a ghost: the composition of the X-face pass (all rows) and
-// the Y-face pass (all columns) of MakeBoundariesFunctor
-// (src/HydroRunFunctors.h:1855-2024).  Reflect mirrors (2g-1-i) and flips
-// the normal momentum, absorb copies the first interior cell, periodic
-// wraps.  The result is always an interior cell (nx, ny >= 2).
 __device__ __forceinline__ int src_lo_hi(int i, int n, int bc_lo, int bc_hi, bool &flip) {
-  flip = false;
-  if (i < 2) {
-    if (bc_lo == E2D_BC_REFLECT) {
-      flip = true;
-      return 3 - i;
-    }
-    if (bc_lo == E2D_BC_ABSORB) return 2;
-    return n + i;
-  }
-  if (i >= n + 2) {
-    if (bc_hi == E2D_BC_REFLECT) {
-      flip = true;
-      return 2 * n + 3 - i;
-    }
-    if (bc_hi == E2D_BC_ABSORB) return n + 1;
-    return i - n;
-  }
-  return i;
+  return ghost_source(i, n, bc_lo, bc_hi, flip);
 }
-
-__device__ __forceinline__ bool nonfinite(double x) {
-  return ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
-}
+__device__ __forceinline__ bool nonfinite(double x) { return nonfinite64(x); }
 
 // ------------------------------------------------------------ numerics
-// src/HydroBaseFunctor.h:421-455, one direction.
-__device__ __forceinline__ double slope_1d(double st, double q, double qp, double qm) {
-  const double dlft = st * (q - qm);
-  const double drgt = st * (qp - q);
-  const double dcen = 0.5 * (qp - qm);
-  const double dsgn = (dcen >= 0.0) ? 1.0 : -1.0;
-  const double slop = fmin(fabs(dlft), fabs(drgt));
-  const double dlim = ((dlft * drgt) <= 0.0) ? 0.0 : slop;
-  return dsgn * fmin(dlim, fabs(dcen));
+// src/HydroBaseFunctor.h:76-102 (computePrimitives) without the sound speed.
+__device__ __forceinline__ void primitives(const KPhys<double> &ph, double rho, double e, double mx,
+                                           double my, double &d, double &p, double &ux, double &uy) {
+  d = max_pos(rho, ph.smallr);
+  ux = mx / d;
+  uy = my / d;
+  const double eken = half(ux * ux + uy * uy);
+  const double ei = e / d - eken;
+  p = max_pos(ph.gm1 * d * ei, d * ph.smallp);
+}
+
+// src/HydroBaseFunctor.h:475-516 for one variable and direction: slope_type
+// 0 gives a zero slope, 1 and 2 the limited slope.
+__device__ __forceinline__ double slope(int st_kind, double q, double qp, double qm) {
+  if (st_kind == 0) return 0.0;
+  return f64x::slope_limited(st_kind == 2, q, qp, qm);
+}
+
+// Sources of trace_unsplit_2d_along_dir (src/HydroBaseFunctor.h:246-249).
+__device__ __forceinline__ void trace_sources(const KPhys<double> &ph, const double q[4],
+                                              const double dqx[4], const double dqy[4], double s0[4]) {
+  const double r = q[E2D_ID], p = q[E2D_IP], u = q[E2D_IU], v = q[E2D_IV];
+  const double drx = dqx[E2D_ID], dpx = dqx[E2D_IP], dux = dqx[E2D_IU], dvx = dqx[E2D_IV];
+  const double dry = dqy[E2D_ID], dpy = dqy[E2D_IP], duy = dqy[E2D_IU], dvy = dqy[E2D_IV];
+  s0[E2D_ID] = -u * drx - v * dry - (dux + dvy) * r;
+  s0[E2D_IP] = -u * dpx - v * dpy - (dux + dvy) * ph.gamma0 * p;
+  s0[E2D_IU] = -u * dux - v * duy - (dpx) / r;
+  s0[E2D_IV] = -u * dvx - v * dvy - (dpy) / r;
+}
+
+// The two face states of one direction (src/HydroBaseFunctor.h:251-289):
+// minus face q - dq/2 + s0*dtd/2, plus face q + dq/2 + s0*dtd/2, density
+// clamped at smallr.
+__device__ __forceinline__ void face_pair(const KPhys<double> &ph, int v, double q, double dq,
+                                          double s0, double dtd, double &fm, double &fp) {
+  const double h = half(dq);
+  const double sx = half(s0 * dtd);
+  fm = q - h + sx;
+  fp = q + h + sx;
+  if (v == E2D_ID) {
+    fm = max_pos(fm, ph.smallr);
+    fp = max_pos(fp, ph.smallr);
+  }
 }
 
 // src/HydroBaseFunctor.h:523-547.
@@ -156,31 +173,35 @@ __device__ __noinline__ void riemann_approx(const KPhys<double> &ph, const doubl
 
 // src/HydroBaseFunctor.h:704-809 (riemann_hllc).  The reference builds the
 // star states of both sides and keeps one; this builds only the side the
-// contact selects (ustar > 0: left), which yields the same value.
+// contact selects (ustar > 0: left), which yields the same value.  Cut-offs,
+// maxima, the 0.5 factors and the sign tests use the exact integer forms of
+// e2d_f64_exact.cuh.
 __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const double *ql,
                                              const double *qr, double *flux) {
-  const double rl = fmax(ql[E2D_ID], ph.smallr);
-  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
+  const double rl = max_pos(ql[E2D_ID], ph.smallr);
+  const double pl = max_pos(ql[E2D_IP], rl * ph.smallp);
   const double ul = ql[E2D_IU];
-  double ecinl = 0.5 * rl * ul * ul;
-  ecinl = ecinl + 0.5 * rl * ql[E2D_IV] * ql[E2D_IV];
+  const double hrl = half(rl);
+  double ecinl = hrl * ul * ul;
+  ecinl = ecinl + hrl * ql[E2D_IV] * ql[E2D_IV];
   const double etotl = pl * ph.entho + ecinl;
-  const double rr = fmax(qr[E2D_ID], ph.smallr);
-  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
+  const double rr = max_pos(qr[E2D_ID], ph.smallr);
+  const double pr = max_pos(qr[E2D_IP], rr * ph.smallp);
   const double ur = qr[E2D_IU];
-  double ecinr = 0.5 * rr * ur * ur;
-  ecinr = ecinr + 0.5 * rr * qr[E2D_IV] * qr[E2D_IV];
+  const double hrr = half(rr);
+  double ecinr = hrr * ur * ur;
+  ecinr = ecinr + hrr * qr[E2D_IV] * qr[E2D_IV];
   const double etotr = pr * ph.entho + ecinr;
-  const double cfastl = sqrt(fmax(ph.gamma0 * pl / rl, ph.smallc2));
-  const double cfastr = sqrt(fmax(ph.gamma0 * pr / rr, ph.smallc2));
-  const double cmax = fmax(cfastl, cfastr);
-  const double SL = fmin(ul, ur) - cmax;
-  const double SR = fmax(ul, ur) + cmax;
+  const double cfastl = sqrt(max_pos(ph.gamma0 * pl / rl, ph.smallc2));
+  const double cfastr = sqrt(max_pos(ph.gamma0 * pr / rr, ph.smallc2));
+  const double cmax = max_nn(cfastl, cfastr);
+  const double SL = min_any(ul, ur) - cmax;
+  const double SR = max_any(ul, ur) + cmax;
   const double rcl = rl * (ul - SL);
   const double rcr = rr * (SR - ur);
   const double ustar = (rcr * ur + rcl * ul + (pl - pr)) / (rcr + rcl);
   const double ptotstar = (rcr * pl + rcl * pr + rcl * rcr * (ul - ur)) / (rcr + rcl);
-  const bool lft = ustar > 0.0;
+  const bool lft = gt0(ustar);
   const double S = lft ? SL : SR;
   const double rs = lft ? rl : rr, us = lft ? ul : ur, ps = lft ? pl : pr;
   const double es = lft ? etotl : etotr;
@@ -189,9 +210,9 @@ __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const doub
   const double rstar = rs * sdu / sds;
   const double etotstar = (sdu * es - ps * us + ptotstar * ustar) / sds;
   double ro, uo, ptoto, etoto;
-  if (SL > 0.0) {
+  if (gt0(SL)) {
     ro = rl, uo = ul, ptoto = pl, etoto = etotl;
-  } else if (lft || SR > 0.0) {
+  } else if (lft || gt0(SR)) {
     ro = rstar, uo = ustar, ptoto = ptotstar, etoto = etotstar;
   } else {
     ro = rr, uo = ur, ptoto = pr, etoto = etotr;
@@ -199,7 +220,7 @@ __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const doub
   flux[E2D_ID] = ro * uo;
   flux[E2D_IU] = flux[E2D_ID] * uo + ptoto;
   flux[E2D_IP] = (etoto + ptoto) * uo;
-  flux[E2D_IV] = (flux[E2D_ID] > 0.0) ? flux[E2D_ID] * ql[E2D_IV] : flux[E2D_ID] * qr[E2D_IV];
+  flux[E2D_IV] = gt0(flux[E2D_ID]) ? flux[E2D_ID] * ql[E2D_IV] : flux[E2D_ID] * qr[E2D_IV];
 }
 
 // HLL flux (Harten, Lax, van Leer; Toro, "Riemann Solvers and Numerical
@@ -208,23 +229,24 @@ __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const doub
 // wave speeds.  Operation order matches the oracle's riemann_hll.
 __device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const double *ql,
                                             const double *qr, double *flux) {
-  const double rl = fmax(ql[E2D_ID], ph.smallr);
-  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
+  const double rl = max_pos(ql[E2D_ID], ph.smallr);
+  const double pl = max_pos(ql[E2D_IP], rl * ph.smallp);
   const double ul = ql[E2D_IU], vl = ql[E2D_IV];
-  const double rr = fmax(qr[E2D_ID], ph.smallr);
-  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
+  const double rr = max_pos(qr[E2D_ID], ph.smallr);
+  const double pr = max_pos(qr[E2D_IP], rr * ph.smallp);
   const double ur = qr[E2D_IU], vr = qr[E2D_IV];
-  double ecinl = 0.5 * rl * ul * ul;
-  ecinl = ecinl + 0.5 * rl * vl * vl;
+  const double hrl = half(rl), hrr = half(rr);
+  double ecinl = hrl * ul * ul;
+  ecinl = ecinl + hrl * vl * vl;
   const double etotl = pl * ph.entho + ecinl;
-  double ecinr = 0.5 * rr * ur * ur;
-  ecinr = ecinr + 0.5 * rr * vr * vr;
+  double ecinr = hrr * ur * ur;
+  ecinr = ecinr + hrr * vr * vr;
   const double etotr = pr * ph.entho + ecinr;
-  const double cfastl = sqrt(fmax(ph.gamma0 * pl / rl, ph.smallc2));
-  const double cfastr = sqrt(fmax(ph.gamma0 * pr / rr, ph.smallc2));
-  const double cmax = fmax(cfastl, cfastr);
-  const double SL = fmin(ul, ur) - cmax;
-  const double SR = fmax(ul, ur) + cmax;
+  const double cfastl = sqrt(max_pos(ph.gamma0 * pl / rl, ph.smallc2));
+  const double cfastr = sqrt(max_pos(ph.gamma0 * pr / rr, ph.smallc2));
+  const double cmax = max_nn(cfastl, cfastr);
+  const double SL = min_any(ul, ur) - cmax;
+  const double SR = max_any(ul, ur) + cmax;
   const double UL[4] = {rl, etotl, rl * ul, rl * vl};
   const double UR[4] = {rr, etotr, rr * ur, rr * vr};
   double FL[4], FR[4];
@@ -236,10 +258,10 @@ __device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const doubl
   FR[E2D_IP] = (etotr + pr) * ur;
   FR[E2D_IU] = UR[E2D_IU] * ur + pr;
   FR[E2D_IV] = UR[E2D_IU] * vr;
-  if (SL > 0.0) {
+  if (gt0(SL)) {
 #pragma unroll
     for (int v = 0; v < 4; ++v) flux[v] = FL[v];
-  } else if (SR <= 0.0) {
+  } else if (f64x::le0(SR)) {
 #pragma unroll
     for (int v = 0; v < 4; ++v) flux[v] = FR[v];
   } else {
@@ -301,13 +323,8 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
       }
     }
     if (mode & (FILL_WRITE_Q | FILL_DT)) {
-      // src/HydroBaseFunctor.h:76-102 (computePrimitives)
-      const double dd = fmax(rho, ph.smallr);
-      const double ux = mx / dd;
-      const double uy = my / dd;
-      const double eken = 0.5 * (ux * ux + uy * uy);
-      const double ei = e / dd - eken;
-      const double p = fmax(ph.gm1 * dd * ei, dd * ph.smallp);
+      double dd, p, ux, uy;
+      primitives(ph, rho, e, mx, my, dd, p, ux, uy);
       if (mode & FILL_WRITE_Q) {
         q[d] = dd;
         q[d + g.plane] = p;
@@ -401,7 +418,7 @@ __global__ void __launch_bounds__(NT, 2)
 
   // stage 2: slopes, trace sources and face states of the tile cells and of
   // the 1-cell ring (corners excluded) -- src/HydroBaseFunctor.h:214-291
-  const double st = ph.slope_type;
+  const int st_kind = (ph.slope_type == 2.0) ? 2 : (ph.slope_type == 1.0) ? 1 : 0;
   for (int k = tid; k < YH * XW; k += NT) {
     const int yy = k / XW, xx = k - yy * XW;  // cell (xx-1, yy-1) of the tile
     const bool xin = (xx >= 1) && (xx <= TX);
@@ -413,34 +430,17 @@ __global__ void __launch_bounds__(NT, 2)
     for (int v = 0; v < 4; ++v) {
       const double *P = sQ + v * QH * QW;
       qc[v] = P[c];
-      if (st == 0.0) {
-        dqx[v] = 0.0;
-        dqy[v] = 0.0;
-      } else {
-        dqx[v] = slope_1d(st, qc[v], P[c + 1], P[c - 1]);
-        dqy[v] = slope_1d(st, qc[v], P[c + QW], P[c - QW]);
-      }
+      dqx[v] = slope(st_kind, qc[v], P[c + 1], P[c - 1]);
+      dqy[v] = slope(st_kind, qc[v], P[c + QW], P[c - QW]);
     }
-    const double r = qc[E2D_ID], p = qc[E2D_IP], u = qc[E2D_IU], vv = qc[E2D_IV];
-    const double drx = dqx[E2D_ID], dpx = dqx[E2D_IP], dux = dqx[E2D_IU], dvx = dqx[E2D_IV];
-    const double dry = dqy[E2D_ID], dpy = dqy[E2D_IP], duy = dqy[E2D_IU], dvy = dqy[E2D_IV];
     double s0[4];
-    s0[E2D_ID] = -u * drx - vv * dry - (dux + dvy) * r;
-    s0[E2D_IP] = -u * dpx - vv * dpy - (dux + dvy) * ph.gamma0 * p;
-    s0[E2D_IU] = -u * dux - vv * duy - (dpx) / r;
-    s0[E2D_IV] = -u * dvx - vv * dvy - (dpy) / r;
+    trace_sources(ph, qc, dqx, dqy, s0);
     if (yin) {
       const int o = (yy - 1) * XW + xx;
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const double h = 0.5 * dqx[v];
-        const double sx = s0[v] * dtdx * 0.5;
-        double fm = qc[v] - h + sx;
-        double fp = qc[v] + h + sx;
-        if (v == E2D_ID) {
-          fm = fmax(ph.smallr, fm);
-          fp = fmax(ph.smallr, fp);
-        }
+        double fm, fp;
+        face_pair(ph, v, qc[v], dqx[v], s0[v], dtdx, fm, fp);
         if (xx >= 1) sXm[v * TY * XW + o] = fm;
         if (xx <= TX) sXp[v * TY * XW + o] = fp;
       }
@@ -449,14 +449,8 @@ __global__ void __launch_bounds__(NT, 2)
       const int o = yy * TX + (xx - 1);
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const double h = 0.5 * dqy[v];
-        const double sy = s0[v] * dtdy * 0.5;
-        double fm = qc[v] - h + sy;
-        double fp = qc[v] + h + sy;
-        if (v == E2D_ID) {
-          fm = fmax(ph.smallr, fm);
-          fp = fmax(ph.smallr, fp);
-        }
+        double fm, fp;
+        face_pair(ph, v, qc[v], dqy[v], s0[v], dtdy, fm, fp);
         if (yy >= 1) sYm[v * YH * TX + o] = fm;
         if (yy <= TY) sYp[v * YH * TX + o] = fp;
       }
@@ -541,6 +535,58 @@ __global__ void __launch_bounds__(NT, 2)
       clk->done_blocks = 0u;
       __threadfence();
     }
+  }
+}
+
+// ------------------------------------------------------------ building blocks
+// One building block of the step per thread, with the exact device code the
+// step kernels use (see e2d_eval_device in include/e2d.h for the layouts).
+__global__ void k_eval_f64(const KParams64 kp, const int what, const int n,
+                           const double *__restrict__ in, double *__restrict__ out, const double dtdx,
+                           const double dtdy) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const KPhys<double> &ph = kp.ph;
+  const int st_kind = (ph.slope_type == 2.0) ? 2 : (ph.slope_type == 1.0) ? 1 : 0;
+  if (what == E2D_EVAL_PRIMITIVES) {
+    const double *u = in + 4 * k;
+    double d, p, ux, uy;
+    primitives(ph, u[E2D_ID], u[E2D_IP], u[E2D_IU], u[E2D_IV], d, p, ux, uy);
+    double *o = out + 5 * k;
+    o[E2D_ID] = d;
+    o[E2D_IP] = p;
+    o[E2D_IU] = ux;
+    o[E2D_IV] = uy;
+    o[4] = sqrt(ph.gamma0 * p / d);
+  } else if (what == E2D_EVAL_SLOPES) {
+    const double *s = in + 20 * k;  // q, q(+x), q(-x), q(+y), q(-y)
+    double *o = out + 8 * k;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      o[v] = slope(st_kind, s[v], s[4 + v], s[8 + v]);
+      o[4 + v] = slope(st_kind, s[v], s[12 + v], s[16 + v]);
+    }
+  } else if (what >= E2D_EVAL_TRACE_XMIN && what <= E2D_EVAL_TRACE_YMAX) {
+    const double *s = in + 12 * k;  // q, dqx, dqy
+    double s0[4];
+    trace_sources(ph, s, s + 4, s + 8, s0);
+    const int face = what - E2D_EVAL_TRACE_XMIN;
+    const bool xdir = face < 2;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double fm, fp;
+      face_pair(ph, v, s[v], xdir ? s[4 + v] : s[8 + v], s0[v], xdir ? dtdx : dtdy, fm, fp);
+      out[4 * k + v] = (face == 0 || face == 2) ? fm : fp;
+    }
+  } else {
+    const double *s = in + 8 * k;  // qleft, qright
+    double *o = out + 4 * k;
+    if (what == E2D_EVAL_RIEMANN_HLLC)
+      riemann_hllc(ph, s, s + 4, o);
+    else if (what == E2D_EVAL_RIEMANN_HLL)
+      riemann_hll(ph, s, s + 4, o);
+    else
+      riemann_approx(ph, s, s + 4, o);
   }
 }
 
@@ -670,6 +716,13 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
     default:
       return launch_flux_t<E2D_RIEMANN_APPROX>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
   }
+}
+
+cudaError_t launch_eval_f64(const KParams64 &kp, int what, int n, const double *in, double *out,
+                            double dtdx, double dtdy, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_eval_f64<<<(n + 127) / 128, 128, 0, s>>>(kp, what, n, in, out, dtdx, dtdy);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_init_f64(const KParams64 &kp, const e2d_params &p, double *u, cudaStream_t s) {

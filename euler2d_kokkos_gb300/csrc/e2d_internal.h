@@ -55,6 +55,13 @@ struct KParams64 {
   KPhys<double> ph;
 };
 
+// FP32 step with FP64 copies of the constants the exact dt recompute uses.
+struct KParams32 {
+  KGeom g;
+  KPhys<float> ph;
+  KPhys<double> ph64;
+};
+
 // Device-resident loop state of the time loop of src/main.cpp:100-145.
 struct DevClock {
   double t;                       // simulated time
@@ -67,6 +74,9 @@ struct DevClock {
   unsigned int done_blocks;       // blocks of the current step kernel that finished
   unsigned int status;            // E2D_FLAG_* bits seen by the device
   unsigned int fill_count;        // blocks of the current primitives kernel that finished
+  // FP32 path: the step of parity n reads the CFL maximum of its input from
+  // acc[n & 1] and folds that of its output into acc[(n + 1) & 1]
+  unsigned long long acc[2];
 };
 
 enum : unsigned int {
@@ -97,6 +107,31 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
 // launch or graph capture.
 cudaError_t configure_f64_kernels();
 cudaError_t launch_init_f64(const KParams64 &kp, const e2d_params &p, double *u, cudaStream_t s);
+cudaError_t launch_eval_f64(const KParams64 &kp, int what, int n, const double *in, double *out,
+                            double dtdx, double dtdy, cudaStream_t s);
+void make_kparams(const e2d_params &p, KParams64 *kp);
+void make_kparams32(const e2d_params &p, KParams32 *kp);
+
+// FP32 path with compensated (hi, lo) state (e2d_fp32c.cu).  A state is 8
+// float planes of isize*jsize: hi(rho, E, mx, my) then lo(rho, E, mx, my).
+// Ghost cells of these arrays are not maintained: the step reads ghosts
+// through the boundary map.
+cudaError_t configure_f32c_kernels();
+cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w, cudaStream_t s);
+cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, cudaStream_t s);
+// CFL maximum of a state (interior) into clk->acc[slot] (slot < 0: invdt_bits).
+cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s);
+cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
+                             DevClock *clk, int use_clock, double host_dt, double *dt_trace,
+                             cudaStream_t s);
+
+// FP64 reductions over the interior (e2d_reduce.cu): per-variable sums and
+// the L1 difference of two states, deterministic (fixed summation tree).
+// `partial` holds at least reduce_partial_count(p) doubles.
+size_t reduce_partial_count(const KGeom &g);
+cudaError_t launch_sums_f64(const KGeom &g, const double *u, double *partial, double *out4, cudaStream_t s);
+cudaError_t launch_l1diff_f64(const KGeom &g, const double *a, const double *b, int var,
+                              double *partial, double *out2, cudaStream_t s);
 size_t flux_update_f64_smem_bytes();
 
 }  // namespace e2d

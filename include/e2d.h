@@ -165,6 +165,33 @@ int e2d_godunov_unsplit(e2d_sim *sim, int nStep, double dt);
  * replayed from cached CUDA graphs.  Blocks until done. */
 int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double *dt_trace);
 
+/* Building blocks of the FP64 step evaluated on the device, n independent
+ * inputs each (host arrays; the per-function known-answer interface of the
+ * reference's HydroBaseFunctor, src/HydroBaseFunctor.h):
+ *   E2D_EVAL_PRIMITIVES   in 4/item (rho,E,mx,my)        out 5 (rho,p,u,v,c)
+ *                         -- computePrimitives, :76-102
+ *   E2D_EVAL_SLOPES       in 20/item (q,q+x,q-x,q+y,q-y) out 8 (dqx, dqy)
+ *                         -- slope_unsplit_hydro_2d, :475-516
+ *   E2D_EVAL_TRACE_*      in 12/item (q, dqx, dqy)       out 4 (face state)
+ *                         -- trace_unsplit_2d_along_dir, :214-291
+ *   E2D_EVAL_RIEMANN_*    in 8/item (qleft, qright)      out 4 (flux)
+ *                         -- riemann_approx :558-693, riemann_hllc :704-809,
+ *                            and the HLL flux this build adds.
+ * dtdx / dtdy are used by the trace only. */
+enum {
+  E2D_EVAL_PRIMITIVES = 0,
+  E2D_EVAL_SLOPES = 1,
+  E2D_EVAL_TRACE_XMIN = 2,
+  E2D_EVAL_TRACE_XMAX = 3,
+  E2D_EVAL_TRACE_YMIN = 4,
+  E2D_EVAL_TRACE_YMAX = 5,
+  E2D_EVAL_RIEMANN_APPROX = 6,
+  E2D_EVAL_RIEMANN_HLL = 7,
+  E2D_EVAL_RIEMANN_HLLC = 8
+};
+int e2d_eval_device(const e2d_params *p, int what, int n, const double *in, double *out, double dtdx,
+                    double dtdy);
+
 /* Per-kernel device time: with profiling on, e2d_step_n launches kernels
  * directly with CUDA events around each one.  names/ms/launches receive, per
  * kernel, its name, total milliseconds and launch count. */

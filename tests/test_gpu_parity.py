@@ -190,6 +190,72 @@ def test_nonfinite_state_reports_enumeric(gpu_lib, tmp_path):
         assert h2.compute_dt(0) > 0
 
 
+def _kat_device_params(kat, key, tmp_path):
+    return e2d.HydroParams.from_ini(C.write_ini(str(kat[key]), str(tmp_path), "kat.ini"))
+
+
+def test_device_primitives_kat(gpu_lib, kat, tmp_path):
+    p = _kat_device_params(kat, "ini_slope2", tmp_path)
+    out = e2d.eval_device(p, "primitives", kat["prim_u"])
+    assert np.array_equal(out[:, :4], kat["prim_q"])
+    assert np.array_equal(out[:, 4], kat["prim_c"])
+
+
+@pytest.mark.parametrize("st", [1, 2])
+def test_device_slopes_kat(gpu_lib, kat, tmp_path, st):
+    p = _kat_device_params(kat, f"ini_slope{st}", tmp_path)
+    out = e2d.eval_device(p, "slopes", kat["slope_q5"])
+    assert np.array_equal(out[:, :4], kat[f"slope{st}_dqx"])
+    assert np.array_equal(out[:, 4:], kat[f"slope{st}_dqy"])
+
+
+@pytest.mark.parametrize("face,name", [(0, "trace_xmin"), (1, "trace_xmax"), (2, "trace_ymin"),
+                                       (3, "trace_ymax")])
+def test_device_trace_kat(gpu_lib, kat, tmp_path, face, name):
+    p = _kat_device_params(kat, "ini_slope2", tmp_path)
+    x = np.concatenate([kat["trace_q"], kat["trace_dqx"], kat["trace_dqy"]], axis=1)
+    out = e2d.eval_device(p, name, x, float(kat["trace_dtdx"]), float(kat["trace_dtdy"]))
+    assert np.array_equal(out, kat[f"trace_face{face}"])
+
+
+@pytest.mark.parametrize("solver", ["hllc", "approx"])
+def test_device_riemann_kat(gpu_lib, kat, tmp_path, solver):
+    p = _kat_device_params(kat, "ini_slope2", tmp_path)
+    x = np.concatenate([kat["riemann_ql"], kat["riemann_qr"]], axis=1)
+    out = e2d.eval_device(p, f"riemann_{solver}", x)
+    assert np.array_equal(out, kat[f"riemann_{solver}"])
+
+
+def test_device_hll_vs_oracle(gpu_lib, kat, tmp_path):
+    p = _kat_device_params(kat, "ini_slope2", tmp_path)
+    x = np.concatenate([kat["riemann_ql"], kat["riemann_qr"]], axis=1)
+    out = e2d.eval_device(p, "riemann_hll", x)
+    op = po.make_params(**C.oracle_kwargs(str(kat["ini_slope2"])))
+    assert np.array_equal(out, po.riemann(op, "hll", kat["riemann_ql"], kat["riemann_qr"]))
+
+
+def test_device_slopes_edge_values(gpu_lib, tmp_path):
+    """Exact integer-pipe limiter on signed zeros, ties, tiny and subnormal
+    differences, compared with the oracle's plain FP64 expression."""
+    vals = np.array([0.0, -0.0, 1.0, -1.0, 1e-300, -1e-300, 5e-324, -5e-324, 2.2250738585072014e-308,
+                     1e-160, -1e-160, 3.0, 0.5, 1.0 + 2 ** -52, 1e300])
+    rng = np.random.default_rng(17)
+    idx = rng.integers(0, len(vals), size=(3000, 3))
+    q5 = np.zeros((3000, 5, 4))
+    q5[:, 0, :] = vals[idx[:, 0]][:, None]
+    q5[:, 1, :] = vals[idx[:, 1]][:, None]
+    q5[:, 2, :] = vals[idx[:, 2]][:, None]
+    q5[:, 3, :] = vals[idx[:, 2]][:, None]
+    q5[:, 4, :] = vals[idx[:, 1]][:, None]
+    for st in (1, 2):
+        text = C.ini_text(8, 8, slope_type=st)
+        p = e2d.HydroParams.from_ini(C.write_ini(text, str(tmp_path), f"s{st}.ini"))
+        out = e2d.eval_device(p, "slopes", q5)
+        dqx, dqy = po.slopes(po.make_params(**C.oracle_kwargs(text)), q5)
+        np.testing.assert_array_equal(out[:, :4].view(np.int64), dqx.view(np.int64))
+        np.testing.assert_array_equal(out[:, 4:].view(np.int64), dqy.view(np.int64))
+
+
 def test_profiling_mode_same_bits(gpu_lib, runs, tmp_path):
     name = "blast_reflect"
     text = str(runs[f"{name}__ini"])
