@@ -1,13 +1,20 @@
 """Benchmark of the GB300 unsplit MUSCL-Hancock Godunov step.
 
-Workload: the 4096x4096 blast (gamma 1.4, reflecting walls, rho = 1, p = 10
-inside a disc of radius 0.125 at (0.5, 0.5), p = 0.1 outside, HLLC, CFL 0.8),
-FP64.  One step = one time step of the device time loop (dt from the CFL
-maximum of the current state, clamped at t_end; ghost fill, primitives,
-slopes, trace, Riemann solves, conservative update).  The state (2 x 537 MB)
-is larger than L2, so every step streams it from HBM.
+Headline workload (default): the 4096x4096 blast in FP64 -- gamma 1.4,
+reflecting walls, rho = 1, p = 10 inside a disc of radius 0.125 at
+(0.5, 0.5), p = 0.1 outside, HLLC, CFL 0.8.  One step = one time step of the
+device time loop (dt from the CFL maximum of the current state, clamped at
+t_end; ghost fill, primitives, slopes, trace, Riemann solves, conservative
+update).  The state (2 x 537 MB) is larger than L2, so every step streams it
+from HBM.
+
+Secondary (in the same JSON line, key "fp32c"): the 8192x8192 four-quadrant
+Riemann problem (Lax-Liu 3 split at 0.5, absorbing walls, HLLC, CFL 0.8) in
+the FP32 compensated mode, with its relative L1 density error against the
+FP64 path (which is bit-identical to the reference) at 1024x1024, t = 0.3.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--precision fp64|fp32c] [--problem blast|four_quadrant] [--nx N]
 
 Prints one JSON line.  `--impl reference` times the reference algorithm on
 the host cores instead: the CPU oracle (a restatement of the reference's own
@@ -30,7 +37,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "Gcell-updates/s"
 HBM_FALLBACK_GBS = 6800.0
-BYTES_PER_CELL = {"fp64": 64}  # read U + write U, 4 variables
+BYTES_PER_CELL = {"fp64": 64, "fp32c": 64}  # read + write of the 4 conserved variables
+BLAST = dict(blast_radius=0.125, blast_center_x=0.5, blast_center_y=0.5, blast_density_in=1.0,
+             blast_density_out=1.0, blast_pressure_in=10.0, blast_pressure_out=0.1)
 
 
 def parse():
@@ -39,31 +48,47 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--nx", type=int, default=4096)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"])
+    ap.add_argument("--problem", default=None, choices=["blast", "four_quadrant"])
+    ap.add_argument("--nx", type=int, default=None)
     ap.add_argument("--riemann", default="hllc", choices=["hllc", "hll", "approx"])
     ap.add_argument("--cpu-sample-steps", type=int, default=0,
                     help="steps of the CPU baseline sample (0: sized to ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--no-secondary", action="store_true")
+    a = ap.parse_args()
+    if a.problem is None:
+        a.problem = "blast" if a.precision == "fp64" else "four_quadrant"
+    if a.nx is None:
+        a.nx = 4096 if a.problem == "blast" else 8192
+    return a
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def workload_params(e2d, nx, riemann):
-    return e2d.make_params(nx, nx, problem="blast", riemann=riemann, gamma0=1.4, cfl=0.8,
-                           slope_type=2.0, bc=(1, 1, 1, 1), blast_radius=0.125,
-                           blast_center_x=0.5, blast_center_y=0.5, blast_density_in=1.0,
-                           blast_density_out=1.0, blast_pressure_in=10.0, blast_pressure_out=0.1)
+def workload_params(e2d, problem, nx, riemann, precision):
+    prec = e2d.PRECISION_FP64 if precision == "fp64" else e2d.PRECISION_FP32C
+    if problem == "blast":
+        return e2d.make_params(nx, nx, problem="blast", riemann=riemann, gamma0=1.4, cfl=0.8,
+                               slope_type=2.0, bc=(1, 1, 1, 1), precision=prec, **BLAST)
+    return e2d.make_params(nx, nx, problem="four_quadrant", riemann=riemann, gamma0=1.4, cfl=0.8,
+                           slope_type=2.0, bc=(2, 2, 2, 2), precision=prec, fq_split_x=0.5,
+                           fq_split_y=0.5)
 
 
-def config(nx, riemann, extra=None):
-    c = {"workload": f"blast {nx}x{nx}, FP64, {riemann.upper()}, reflecting walls, CFL 0.8",
-         "nx": nx, "ny": nx, "riemann": riemann, "precision": "fp64",
+def workload_name(problem, nx, riemann, precision):
+    if problem == "blast":
+        return f"blast {nx}x{nx}, {precision.upper()}, {riemann.upper()}, reflecting walls, CFL 0.8"
+    return (f"four-quadrant (Lax-Liu 3, split 0.5) {nx}x{nx}, {precision.upper()}, {riemann.upper()}, "
+            f"absorbing walls, CFL 0.8")
+
+
+def config(problem, nx, riemann, precision, extra=None):
+    c = {"workload": workload_name(problem, nx, riemann, precision), "nx": nx, "ny": nx,
+         "riemann": riemann, "precision": precision,
          "l2": f"state {4 * (nx + 4) ** 2 * 8 / 1e6:.0f} MB per array > 129 MB L2 (no flush needed)",
          "parallelism": "replicas"}
     if extra:
@@ -81,16 +106,13 @@ def measured_peaks():
     return {"hbm_gbs": HBM_FALLBACK_GBS}, "fallback"
 
 
-def ncu_traffic(kernel_prefix):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary, scaled to the benchmark's grid (profiles/*.json)."""
+def ncu_traffic(kernel):
+    """DRAM bytes per cell of a kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     try:
-        d = json.load(open(path))
-        e = d.get(kernel_prefix)
-        return e
+        return json.load(open(path)).get(kernel)
     except Exception:
         return None
 
@@ -132,7 +154,7 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
-        sm, mx, reasons = [], None, set()
+        sm, mx, reasons, power = [], None, set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
@@ -141,6 +163,7 @@ class ClockSampler:
             try:
                 sm.append(float(parts[1]))
                 mx = float(parts[2])
+                power.append(float(parts[3]))
             except ValueError:
                 continue
             for nm, val in zip(names, parts[5:9]):
@@ -149,19 +172,27 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "power_w_max": max(power) if power else None}
 
 
-def cpu_baseline(nx, riemann, steps, label_sample=True):
-    """The oracle (reference FP64 algorithm, OpenMP) on the host cores."""
+def oracle_setup(problem, nx, riemann):
     from oracle import pyoracle as po
 
-    p = po.make_params(nx, nx, gamma0=1.4, cfl=0.8, slope_type=2.0, bc=(1, 1, 1, 1), riemann=riemann)
-    u0 = po.init_blast(p, radius=po.f32(0.125), cx=po.f32(0.5), cy=po.f32(0.5), d_in=1.0,
-                       d_out=1.0, p_in=10.0, p_out=po.f32(0.1))
+    if problem == "blast":
+        p = po.make_params(nx, nx, gamma0=1.4, cfl=0.8, slope_type=2.0, bc=(1, 1, 1, 1), riemann=riemann)
+        u0 = po.init_blast(p, radius=po.f32(0.125), cx=po.f32(0.5), cy=po.f32(0.5), d_in=1.0,
+                           d_out=1.0, p_in=10.0, p_out=po.f32(0.1))
+    else:
+        p = po.make_params(nx, nx, gamma0=1.4, cfl=0.8, slope_type=2.0, bc=(2, 2, 2, 2), riemann=riemann)
+        u0 = po.init_four_quadrant(p, xt=po.f32(0.5), yt=po.f32(0.5))
+    return po, p, u0
+
+
+def cpu_baseline(problem, nx, steps):
+    """The oracle (reference FP64 algorithm, OpenMP) on the host cores."""
+    po, p, u0 = oracle_setup(problem, nx, "hllc")
     threads = po.lib().orc_num_threads()
-    if steps <= 0:
-        # size the sample to roughly 15 s of CPU time
+    if steps <= 0:  # size the sample to roughly 15 s of CPU time
         t0 = time.perf_counter()
         po.run(p, u0, 1, 10.0)
         one = time.perf_counter() - t0
@@ -170,47 +201,162 @@ def cpu_baseline(nx, riemann, steps, label_sample=True):
     _, _, _, ns = po.run(p, u0, steps, 10.0)
     el = time.perf_counter() - t0
     return {"value": nx * nx * ns / el / 1e9, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{ns} time steps of the {nx}x{nx} blast (oracle restatement of the "
-                      f"reference's FP64 impl-0 step, OpenMP over {threads} threads), {el:.1f} s"}
+            "sample": f"{ns} time steps of the {nx}x{nx} {problem} (oracle restatement of the "
+                      f"reference's FP64 implementation-0 step, OpenMP over {threads} threads), {el:.1f} s"}
 
 
-def run_reference_arm(args, rank, world):
+def run_reference_arm(args, rank):
     if rank != 0:
         return
-    from oracle import pyoracle as po
-
-    nx = args.nx
-    p = po.make_params(nx, nx, gamma0=1.4, cfl=0.8, slope_type=2.0, bc=(1, 1, 1, 1), riemann="hllc")
-    u = po.init_blast(p, radius=po.f32(0.125), cx=po.f32(0.5), cy=po.f32(0.5), d_in=1.0, d_out=1.0,
-                      p_in=10.0, p_out=po.f32(0.1))
-    u2 = u.copy()
+    po, p, u = oracle_setup(args.problem, args.nx, "hllc")
     if args.warmup > 0:
         u, _, _, _ = po.run(p, u, args.warmup, 10.0)
-        u2 = u.copy()
     threads = po.lib().orc_num_threads()
     t0 = time.perf_counter()
     _, dts, _, ns = po.run(p, u, args.steps, 10.0)
     el = time.perf_counter() - t0
-    value = nx * nx * ns / el / 1e9
+    value = args.nx * args.nx * ns / el / 1e9
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 0, "steps": ns,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / max(ns, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": config(nx, "hllc", {"implementation": "CPU oracle: restatement of the "
-                                          "reference's FP64 implementation-0 step (the reference "
-                                          "runs HLLC whatever the riemann key says)"}),
+            "config": config(args.problem, args.nx, "hllc", "fp64",
+                             {"implementation": "CPU oracle: restatement of the reference's FP64 "
+                                                "implementation-0 step, bit-identical to it (the "
+                                                "reference itself runs HLLC whatever the riemann key says)"}),
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                             "sample": f"{ns} full time steps of the {nx}x{nx} blast"},
+                             "sample": f"{ns} full time steps of the {args.nx}x{args.nx} {args.problem}"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "gpu_launches": 0}
     print(json.dumps(line), flush=True)
+
+
+def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
+            with_e2e=True, with_clocks=True):
+    p = workload_params(e2d, problem, nx, args.riemann, precision)
+    h = e2d.HydroRun(p)
+    stream = torch.cuda.ExternalStream(h.stream())
+    t_end = 10.0
+    t, ns = 0.0, 0
+    if warmup > 0:
+        t, ns, _ = h.step_n(warmup, t_end, t, ns)
+    barrier()
+    # timed region 1: exactly K steps with per-kernel CUDA events on the library's stream
+    h.reset_kernel_times()
+    h.set_profiling(True)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local) if with_clocks else None
+    if sampler:
+        sampler.__enter__()
+    barrier()
+    ev0.record(stream)
+    t, ns, _ = h.step_n(steps, t_end, t, ns)
+    ev1.record(stream)
+    barrier()
+    if sampler:
+        sampler.__exit__(None, None, None)
+    ms_prof = ev0.elapsed_time(ev1)
+    kt = h.kernel_times()
+    h.set_profiling(False)
+    # timed region 2: the same K steps replayed from CUDA graphs (the production path)
+    barrier()
+    ev0.record(stream)
+    t, ns, _ = h.step_n(steps, t_end, t, ns)
+    ev1.record(stream)
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = ms
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = float(tt.item())
+    out = {"ms": ms_max, "ms_profiled": ms_prof, "kernels": kt,
+           "clocks": sampler.summary() if sampler else None}
+    if with_e2e:
+        # end to end through the C ABI with host buffers: upload the initial
+        # state from pinned memory, K steps, read the result back
+        host_in = torch.empty((4, nx + 4, nx + 4), dtype=torch.float64, pin_memory=True).numpy()
+        host_out = torch.empty((4, nx + 4, nx + 4), dtype=torch.float64, pin_memory=True).numpy()
+        h0 = e2d.HydroRun(p)
+        h0.get_state(0, host_in)
+        h0.close()
+        barrier()
+        t0 = time.perf_counter()
+        h.set_state(0, host_in)
+        _, ns2, _ = h.step_n(steps, t_end, 0.0, 0)
+        h.get_state(ns2 % 2, host_out)
+        e2e_s = time.perf_counter() - t0
+        out["e2e"] = {"value": nx * nx * ns2 / e2e_s / 1e9, "unit": METRIC,
+                      "h2d_bytes_per_step": host_in.nbytes / max(ns2, 1),
+                      "d2h_bytes_per_step": (host_out.nbytes + 8 * ns2) / max(ns2, 1),
+                      "path": "e2d_set_state + e2d_step_n + e2d_get_state from pinned host buffers, "
+                              f"{ns2} steps per call"}
+    h.close()
+    return out
+
+
+def roofline(kt, precision, cells, prefix):
+    name = next((k for k in kt if k.startswith(prefix)), None)
+    if not name:
+        return None
+    peaks, kind = measured_peaks()
+    k_ms, k_n = kt[name]
+    avg_s = k_ms / k_n / 1e3
+    alg = BYTES_PER_CELL[precision] * cells
+    achieved = alg / avg_s / 1e9
+    peak = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
+    tr = ncu_traffic(name)
+    r = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+         "traffic": (tr["bytes_per_cell"] * cells) if tr and tr.get("bytes_per_cell") else None,
+         "kernel": name, "kernel_ms_avg": avg_s * 1e3,
+         "algorithmic_bytes_per_launch": alg,
+         "peak_source": ("of measured (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured"
+                         else "of fallback 6.8 TB/s")}
+    if tr:
+        r["traffic_source"] = tr.get("source")
+    return r
+
+
+def fp64_pipe_info(kt, cells):
+    path = os.path.join(ROOT, "profiles", "fp64_peak.json")
+    if not os.path.exists(path):
+        return None
+    d = json.load(open(path))
+    out = {"dfma_peak_gops": d.get("dfma_gops")}
+    busy = d.get("fp64_pipe_busy_pct")
+    if busy:
+        out["fp64_pipe_busy_pct_ncu"] = busy
+    return out
+
+
+def l1_check(e2d, nx, t_end):
+    """FP32C vs FP64 (bit-identical to the reference) on the four-quadrant
+    problem at nx^2 to t_end: relative L1 of density, FP64 accumulation."""
+    hs = {}
+    for prec in ("fp64", "fp32c"):
+        h = e2d.HydroRun(workload_params(e2d, "four_quadrant", nx, "hllc", prec))
+        t, ns = 0.0, 0
+        while t < t_end and ns < 1_000_000:
+            t, ns, tr = h.step_n(512, t_end, t, ns)
+            if len(tr) == 0:
+                break
+        hs[prec] = (h, t, ns)
+    (h64, t64, n64), (h32, t32, n32) = hs["fp64"], hs["fp32c"]
+    d, r = h32.l1_diff(n32 % 2, h64, n64 % 2, e2d.ID)
+    mass0 = None
+    res = {"grid": f"{nx}x{nx}", "t_end": t_end, "steps_fp64": n64, "steps_fp32c": n32,
+           "rel_l1_density_vs_fp64": d / r, "oracle": "FP64 GPU path (bit-identical to the reference)"}
+    for h, _, _ in hs.values():
+        h.close()
+    return res
 
 
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
-        run_reference_arm(args, rank, world)
+        run_reference_arm(args, rank)
         return
 
     import torch
@@ -231,101 +377,42 @@ def main():
         torch.cuda.synchronize()
 
     nx = args.nx
-    p = workload_params(e2d, nx, args.riemann)
-    h = e2d.HydroRun(p)
-    stream = torch.cuda.ExternalStream(h.stream())
-    t_end = 10.0
-    # warm-up: W steps (graph capture happens here)
-    t, ns = 0.0, 0
-    if args.warmup > 0:
-        t, ns, _ = h.step_n(args.warmup, t_end, t, ns)
-    barrier()
-
-    # timed region: exactly K steps, per-kernel CUDA events on the library's stream
-    h.reset_kernel_times()
-    h.set_profiling(True)
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        barrier()
-        ev0.record(stream)
-        t, ns, _ = h.step_n(args.steps, t_end, t, ns)
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1)
-    kt = h.kernel_times()
-    h.set_profiling(False)
-
-    # the same K steps replayed from CUDA graphs (the production path)
-    barrier()
-    ev0.record(stream)
-    t, ns, _ = h.step_n(args.steps, t_end, t, ns)
-    ev1.record(stream)
-    barrier()
-    ms_graph = ev0.elapsed_time(ev1)
-    ms_max = ms_graph
-    if dist:
-        tt = torch.tensor([ms_graph], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
     cells = nx * nx
-    value = cells * args.steps * world / (ms_max / 1e3) / 1e9
-
-    # end to end through the C ABI with host buffers: upload the initial
-    # state from pinned memory, K steps, read the result back
-    host_in = torch.empty((4, nx + 4, nx + 4), dtype=torch.float64, pin_memory=True).numpy()
-    host_out = torch.empty_like(torch.from_numpy(host_in)).pin_memory().numpy()
-    h0 = e2d.HydroRun(p)
-    h0.get_state(0, host_in)
-    h0.close()
-    barrier()
-    t0 = time.perf_counter()
-    h.set_state(0, host_in)
-    t2, ns2, _ = h.step_n(args.steps, t_end, 0.0, 0)
-    h.get_state(ns2 % 2, host_out)
-    e2e_s = time.perf_counter() - t0
-    state_bytes = host_in.nbytes
-    e2e = {"value": cells * ns2 / e2e_s / 1e9, "unit": METRIC,
-           "h2d_bytes_per_step": state_bytes / max(ns2, 1),
-           "d2h_bytes_per_step": (state_bytes + 8 * ns2) / max(ns2, 1),
-           "path": "e2d_set_state + e2d_step_n + e2d_get_state from pinned host buffers"}
-
-    k2_name = next((k for k in kt if k.startswith("k_flux_update")), None)
-    peaks, peak_kind = measured_peaks()
-    roof = None
-    if k2_name:
-        k2_ms, k2_n = kt[k2_name]
-        avg_s = k2_ms / k2_n / 1e3
-        alg_bytes = BYTES_PER_CELL["fp64"] * cells
-        achieved = alg_bytes / avg_s / 1e9
-        peak = float(peaks.get("hbm_gbs", HBM_FALLBACK_GBS))
-        tr = ncu_traffic(k2_name.split("<")[0])
-        traffic = None
-        if tr and tr.get("bytes_per_cell"):
-            traffic = tr["bytes_per_cell"] * cells
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": k2_name,
-                "kernel_ms_avg": avg_s * 1e3, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                if peak_kind == "measured" else "fallback 6.8 TB/s",
-                "note": "FP64 path: limited by the FP64 pipe, see fp64_pipe"}
-        fp64 = json.load(open(os.path.join(ROOT, "profiles", "fp64_peak.json"))) \
-            if os.path.exists(os.path.join(ROOT, "profiles", "fp64_peak.json")) else None
-        if fp64:
-            roof["fp64_pipe"] = {"dfma_peak_gops": fp64.get("dfma_gops"),
-                                 "fp64_ops_per_cell": fp64.get("fp64_ops_per_cell")}
-    kernels = {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()}
+    m = measure(e2d, torch, args, args.precision, args.problem, nx, args.steps, args.warmup, local,
+                barrier, dist)
+    value = cells * args.steps * world / (m["ms"] / 1e3) / 1e9
+    kt = m["kernels"]
+    prefix = "k_flux_update" if args.precision == "fp64" else "k_step_f32c"
+    roof = roofline(kt, args.precision, cells, prefix)
+    if roof and args.precision == "fp64":
+        roof["note"] = "the FP64 step is bound by GB300's FP64 pipe, not HBM: see fp64_pipe"
+        roof["fp64_pipe"] = fp64_pipe_info(kt, cells)
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32 (compensated hi/lo state, FP64 dt)",
             "data": "synthetic", "impl": "gb300",
-            "config": config(nx, args.riemann),
-            "ms_per_step_profiled": ms / args.steps,
-            "kernels": kernels, "roofline": roof, "clocks": clocks.summary(), "e2e": e2e,
+            "config": config(args.problem, nx, args.riemann, args.precision),
+            "ms_per_step_profiled": m["ms_profiled"] / args.steps,
+            "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in kt.items()},
+            "roofline": roof, "clocks": m["clocks"], "e2e": m["e2e"],
             "gpu_launches": int(sum(v[1] for v in kt.values())),
-            "reference_formula_mcell_per_s": (nx + 4) ** 2 * args.steps * world / (ms_max / 1e3) / 1e6}
-    h.close()
+            "reference_formula_mcell_per_s": (nx + 4) ** 2 * args.steps * world / (m["ms"] / 1e3) / 1e6}
+
+    if not args.no_secondary and args.precision == "fp64" and rank == 0:
+        # the FP32 compensated mode on the four-quadrant problem at 8192^2
+        s = measure(e2d, torch, args, "fp32c", "four_quadrant", 8192, args.steps, args.warmup, local,
+                    barrier, None, with_e2e=False, with_clocks=False)
+        sc = 8192 * 8192
+        line["fp32c"] = {
+            "config": config("four_quadrant", 8192, args.riemann, "fp32c"),
+            "value": sc * args.steps / (s["ms"] / 1e3) / 1e9, "unit": METRIC,
+            "ms_per_step": s["ms"] / args.steps,
+            "roofline": roofline(s["kernels"], "fp32c", sc, "k_step_f32c"),
+            "accuracy": l1_check(e2d, 1024, 0.3)}
+
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(nx, "hllc", args.cpu_sample_steps)
+        line["cpu_baseline"] = cpu_baseline(args.problem, min(nx, 4096), args.cpu_sample_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

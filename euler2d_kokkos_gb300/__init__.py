@@ -112,6 +112,8 @@ SIGNATURES = {
     "e2d_godunov_unsplit": ([_V, _I, _D], _I),
     "e2d_step_n": ([_V, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I), _V], _I),
     "e2d_eval_device": ([_P, _I, _I, _V, _V, _D, _D], _I),
+    "e2d_conservation": ([_V, _I, _V], _I),
+    "e2d_l1_diff": ([_V, _I, _V, _I, _I, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
     "e2d_set_profiling": ([_V, _I], _I),
     "e2d_kernel_times": ([_V, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D),
                           ctypes.POINTER(ctypes.c_long), ctypes.POINTER(_I)], _I),
@@ -315,6 +317,21 @@ class HydroRun:
     def current(self, nstep: int) -> np.ndarray:
         """State after nstep steps (U for even nstep, U2 for odd)."""
         return self.get_state(nstep % 2)
+
+    # -- FP64 audits
+    def conservation(self, which: int) -> np.ndarray:
+        """FP64 interior sums of (rho, E, mx, my) of state `which`."""
+        out = np.zeros(4)
+        _check(self._lib.e2d_conservation(self._h, int(which), out.ctypes.data), "conservation", self._h)
+        return out
+
+    def l1_diff(self, which: int, other: "HydroRun", other_which: int, var: int = ID):
+        """(sum |self - other|, sum |other|) of one variable over the interior,
+        accumulated in FP64 on the device."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(self._lib.e2d_l1_diff(self._h, int(which), other._h, int(other_which), int(var),
+                                     ctypes.byref(a), ctypes.byref(b)), "l1_diff", self._h)
+        return a.value, b.value
 
     # -- profiling
     def set_profiling(self, on: bool):

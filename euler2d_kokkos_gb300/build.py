@@ -27,7 +27,8 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 # (source, extra nvcc flags)
 UNITS = [
     ("e2d_fp64.cu", ["--fmad=false"]),
-    ("e2d_fp32c.cu", []),
+    ("e2d_fp32c.cu", ["-use_fast_math"]),
+    ("e2d_reduce.cu", ["--fmad=false"]),
     ("e2d_capi.cu", []),
     ("e2d_config.cpp", ["-x", "cu"]),
 ]

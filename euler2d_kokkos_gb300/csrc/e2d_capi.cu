@@ -1,5 +1,6 @@
 // e2d_capi.cu -- the C ABI of include/e2d.h: simulation handles, device
-// buffers, the HydroRun method mirrors and the graph-replayed time loop.
+// buffers, the HydroRun method mirrors and the graph-replayed time loop, for
+// both arithmetic modes (FP64 bit-identical, FP32 compensated).
 #include "e2d_internal.h"
 
 #include <cstdio>
@@ -14,10 +15,16 @@ using namespace e2d;
 struct e2d_sim {
   e2d_params p{};
   KParams64 kp{};
+  KParams32 kp32{};
+  int fp32 = 0;                       // precision == E2D_PRECISION_FP32C
   int device = 0;
   cudaStream_t stream = nullptr;
-  double *U[2] = {nullptr, nullptr};  // U and U2 of the reference
-  double *Q = nullptr;                // primitives scratch (one full array)
+  double *U[2] = {nullptr, nullptr};  // FP64: U and U2 of the reference
+  double *Q = nullptr;                // FP64: primitives scratch (one full array)
+  float *W[2] = {nullptr, nullptr};   // FP32C: compensated U and U2 (8 float planes)
+  double *stage = nullptr;            // FP32C: FP64 staging array (set/get/init)
+  double *partial = nullptr;          // reduction partials
+  double *red_out = nullptr;          // reduction results (device)
   DevClock *clk = nullptr;            // device loop state
   DevClock *clk_host = nullptr;       // pinned mirror
   double *dt_trace = nullptr;         // device dt trace
@@ -48,9 +55,9 @@ int cuda_fail(e2d_sim *s, cudaError_t e, const char *what) {
   return set_err(s, E2D_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define E2D_CK(sim, call, what)                     \
-  do {                                              \
-    cudaError_t e__ = (call);                       \
+#define E2D_CK(sim, call, what)                               \
+  do {                                                        \
+    cudaError_t e__ = (call);                                 \
     if (e__ != cudaSuccess) return cuda_fail(sim, e__, what); \
   } while (0)
 
@@ -83,7 +90,7 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
 
 namespace {
 
-size_t state_count(const e2d_sim *s) { return (size_t)4 * s->p.isize * s->p.jsize; }
+size_t cells(const e2d_sim *s) { return (size_t)s->p.isize * s->p.jsize; }
 
 // LayoutRight (OpenMP backend) <-> LayoutLeft (CUDA backend) on the host.
 void right_to_left(const e2d_params &p, const double *src, double *dst) {
@@ -99,8 +106,15 @@ void left_to_right(const e2d_params &p, const double *src, double *dst) {
       for (int v = 0; v < 4; ++v) dst[((size_t)i * p.jsize + j) * 4 + v] = src[i + (size_t)p.isize * j + plane * v];
 }
 
+const char *riemann_name(int r) {
+  return r == E2D_RIEMANN_HLLC ? "hllc" : r == E2D_RIEMANN_HLL ? "hll" : "approx";
+}
+
 // Kernels of one step of the device time loop, input buffer `par`.
 cudaError_t enqueue_step(e2d_sim *s, int par) {
+  if (s->fp32)
+    return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1,
+                            0.0, s->dt_trace, s->stream);
   double *in = s->U[par], *out = s->U[par ^ 1];
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK;
   cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream);
@@ -155,6 +169,24 @@ int ensure_trace(e2d_sim *s, int n) {
   return E2D_OK;
 }
 
+// FP64 view of state `which` on the device: the state itself (FP64) or its
+// hi + lo conversion into the staging array (FP32C).
+int fp64_view(e2d_sim *s, int which, double **out) {
+  if (!s->fp32) {
+    *out = s->U[which];
+    return E2D_OK;
+  }
+  E2D_CK(s, launch_f32c_to_f64(s->kp32, s->W[which], s->stage, s->stream), "fp32c to fp64");
+  *out = s->stage;
+  return E2D_OK;
+}
+
+void record_kernel(e2d_sim *s, const std::string &name, float ms) {
+  if (!s->k_count.count(name)) s->k_names.push_back(name);
+  s->k_ms[name] += ms;
+  s->k_count[name] += 1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -169,7 +201,7 @@ const char *e2d_status_string(int status) {
     case E2D_ENUMERIC: return "numerical failure (NaN/Inf state or non-positive dt)";
     case E2D_ETIMEOUT: return "device wait timed out";
     case E2D_ECUDA: return "CUDA error";
-    case E2D_EIO: return "cannot read ini file";
+    case E2D_EIO: return "cannot read or write a file";
     default: return "unknown status";
   }
 }
@@ -213,28 +245,39 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
   std::string msg;
   int rc = params_init(&p, &msg);
   if (rc != E2D_OK) return rc;
-  if (p.precision != E2D_PRECISION_FP64) return E2D_EINVAL;
   e2d_sim *s = new (std::nothrow) e2d_sim();
   if (!s) return E2D_ENOMEM;
   s->p = p;
+  s->fp32 = (p.precision == E2D_PRECISION_FP32C) ? 1 : 0;
   make_kparams(p, &s->kp);
+  make_kparams32(p, &s->kp32);
   auto fail = [&](int status) {
     e2d_destroy(s);
     return status;
   };
   if (cudaGetDevice(&s->device) != cudaSuccess) return fail(E2D_ECUDA);
-  if (configure_f64_kernels() != cudaSuccess) return fail(E2D_ECUDA);
+  if (configure_f64_kernels() != cudaSuccess || configure_f32c_kernels() != cudaSuccess) return fail(E2D_ECUDA);
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(E2D_ECUDA);
-  const size_t bytes = sizeof(double) * state_count(s);
-  for (int k = 0; k < 2; ++k)
-    if (cudaMalloc(&s->U[k], bytes) != cudaSuccess) return fail(E2D_ENOMEM);
-  if (cudaMalloc(&s->Q, bytes) != cudaSuccess) return fail(E2D_ENOMEM);
+  const size_t n = cells(s);
+  if (s->fp32) {
+    for (int k = 0; k < 2; ++k) {
+      if (cudaMalloc(&s->W[k], sizeof(float) * 8 * n) != cudaSuccess) return fail(E2D_ENOMEM);
+      if (cudaMemsetAsync(s->W[k], 0, sizeof(float) * 8 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+    }
+    if (cudaMalloc(&s->stage, sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
+  } else {
+    for (int k = 0; k < 2; ++k) {
+      if (cudaMalloc(&s->U[k], sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
+      if (cudaMemsetAsync(s->U[k], 0, sizeof(double) * 4 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+    }
+    if (cudaMalloc(&s->Q, sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
+    if (cudaMemsetAsync(s->Q, 0, sizeof(double) * 4 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+  }
+  if (cudaMalloc(&s->partial, sizeof(double) * reduce_partial_count(s->kp.g)) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMalloc(&s->red_out, sizeof(double) * 8) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&s->clk, sizeof(DevClock)) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMallocHost(&s->clk_host, sizeof(DevClock)) != cudaSuccess) return fail(E2D_ENOMEM);
   std::memset(s->clk_host, 0, sizeof(DevClock));
-  if (cudaMemsetAsync(s->U[0], 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
-  if (cudaMemsetAsync(s->U[1], 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
-  if (cudaMemsetAsync(s->Q, 0, bytes, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
   if (cudaMemsetAsync(s->clk, 0, sizeof(DevClock), s->stream) != cudaSuccess) return fail(E2D_ECUDA);
   if (ensure_trace(s, 1024) != E2D_OK) return fail(E2D_ENOMEM);
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return fail(E2D_ECUDA);
@@ -247,9 +290,14 @@ int e2d_destroy(e2d_sim *s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (auto &kv : s->graphs) cudaGraphExecDestroy(kv.second);
   for (auto ev : s->ev_pool) cudaEventDestroy(ev);
-  for (int k = 0; k < 2; ++k)
+  for (int k = 0; k < 2; ++k) {
     if (s->U[k]) cudaFree(s->U[k]);
+    if (s->W[k]) cudaFree(s->W[k]);
+  }
   if (s->Q) cudaFree(s->Q);
+  if (s->stage) cudaFree(s->stage);
+  if (s->partial) cudaFree(s->partial);
+  if (s->red_out) cudaFree(s->red_out);
   if (s->clk) cudaFree(s->clk);
   if (s->clk_host) cudaFreeHost(s->clk_host);
   if (s->dt_trace) cudaFree(s->dt_trace);
@@ -274,15 +322,22 @@ int e2d_get_stream(e2d_sim *s, void **stream) {
 
 int e2d_device_state(e2d_sim *s, int which, double **dptr) {
   if (!s || !dptr || (which != 0 && which != 1)) return E2D_EINVAL;
-  *dptr = s->U[which];
+  int rc = fp64_view(s, which, dptr);
+  if (rc != E2D_OK) return rc;
+  if (s->fp32) E2D_CK(s, cudaStreamSynchronize(s->stream), "device_state sync");
   return E2D_OK;
 }
 
 int e2d_init_problem(e2d_sim *s) {
   if (!s) return E2D_EINVAL;
-  E2D_CK(s, launch_init_f64(s->kp, s->p, s->U[0], s->stream), "init problem");
-  E2D_CK(s, cudaMemcpyAsync(s->U[1], s->U[0], sizeof(double) * state_count(s),
-                            cudaMemcpyDeviceToDevice, s->stream), "init copy");
+  if (s->fp32) {
+    E2D_CK(s, launch_init_f64(s->kp, s->p, s->stage, s->stream), "init problem");
+    E2D_CK(s, launch_f32c_from_f64(s->kp32, s->stage, s->W[0], s->stream), "init convert");
+    E2D_CK(s, cudaMemcpyAsync(s->W[1], s->W[0], sizeof(float) * 8 * cells(s), cudaMemcpyDeviceToDevice, s->stream), "init copy");
+  } else {
+    E2D_CK(s, launch_init_f64(s->kp, s->p, s->U[0], s->stream), "init problem");
+    E2D_CK(s, cudaMemcpyAsync(s->U[1], s->U[0], sizeof(double) * 4 * cells(s), cudaMemcpyDeviceToDevice, s->stream), "init copy");
+  }
   E2D_CK(s, cudaStreamSynchronize(s->stream), "init sync");
   return E2D_OK;
 }
@@ -290,16 +345,17 @@ int e2d_init_problem(e2d_sim *s) {
 int e2d_set_state(e2d_sim *s, int which, const double *host, int layout) {
   if (!s || !host || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad set_state args");
   if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return set_err(s, E2D_EINVAL, "bad layout");
-  const size_t n = state_count(s);
-  if (layout == E2D_LAYOUT_LEFT) {
-    E2D_CK(s, cudaMemcpyAsync(s->U[which], host, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream), "set_state copy");
-  } else {
-    std::vector<double> tmp(n);
+  const size_t n = 4 * cells(s);
+  std::vector<double> tmp;
+  const double *src = host;
+  if (layout == E2D_LAYOUT_RIGHT) {
+    tmp.resize(n);
     right_to_left(s->p, host, tmp.data());
-    E2D_CK(s, cudaMemcpyAsync(s->U[which], tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s->stream), "set_state copy");
-    E2D_CK(s, cudaStreamSynchronize(s->stream), "set_state sync");
-    return E2D_OK;
+    src = tmp.data();
   }
+  double *dst = s->fp32 ? s->stage : s->U[which];
+  E2D_CK(s, cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream), "set_state copy");
+  if (s->fp32) E2D_CK(s, launch_f32c_from_f64(s->kp32, s->stage, s->W[which], s->stream), "set_state convert");
   E2D_CK(s, cudaStreamSynchronize(s->stream), "set_state sync");
   return E2D_OK;
 }
@@ -307,13 +363,16 @@ int e2d_set_state(e2d_sim *s, int which, const double *host, int layout) {
 int e2d_get_state(e2d_sim *s, int which, double *host, int layout) {
   if (!s || !host || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad get_state args");
   if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return set_err(s, E2D_EINVAL, "bad layout");
-  const size_t n = state_count(s);
+  const size_t n = 4 * cells(s);
+  double *src = nullptr;
+  int rc = fp64_view(s, which, &src);
+  if (rc != E2D_OK) return rc;
   if (layout == E2D_LAYOUT_LEFT) {
-    E2D_CK(s, cudaMemcpyAsync(host, s->U[which], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
+    E2D_CK(s, cudaMemcpyAsync(host, src, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
     E2D_CK(s, cudaStreamSynchronize(s->stream), "get_state sync");
   } else {
     std::vector<double> tmp(n);
-    E2D_CK(s, cudaMemcpyAsync(tmp.data(), s->U[which], sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
+    E2D_CK(s, cudaMemcpyAsync(tmp.data(), src, sizeof(double) * n, cudaMemcpyDeviceToHost, s->stream), "get_state copy");
     E2D_CK(s, cudaStreamSynchronize(s->stream), "get_state sync");
     left_to_right(s->p, tmp.data(), host);
   }
@@ -323,7 +382,7 @@ int e2d_get_state(e2d_sim *s, int which, double *host, int layout) {
 int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
   if (!s || !filename || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad save_vtk args");
   const e2d_params &p = s->p;
-  std::vector<double> host(state_count(s));
+  std::vector<double> host(4 * cells(s));
   int rc = e2d_get_state(s, which, host.data(), E2D_LAYOUT_LEFT);
   if (rc != E2D_OK) return rc;
   FILE *f = std::fopen(filename, "w");
@@ -344,8 +403,7 @@ int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
   for (int v = 0; v < 4; ++v) {
     std::fprintf(f, "    <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\" >\n", names[v]);
     for (int j = 2; j <= p.jsize - 3; ++j)
-      for (int i = 2; i <= p.isize - 3; ++i)
-        std::fprintf(f, "%g ", host[i + (size_t)p.isize * j + plane * v]);
+      for (int i = 2; i <= p.isize - 3; ++i) std::fprintf(f, "%g ", host[i + (size_t)p.isize * j + plane * v]);
     std::fprintf(f, "\n    </DataArray>\n");
   }
   std::fprintf(f, "    </CellData>\n  </Piece>\n  </ImageData>\n</VTKFile>\n");
@@ -356,6 +414,8 @@ int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
 
 int e2d_make_boundaries(e2d_sim *s, int which) {
   if (!s || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad make_boundaries args");
+  // FP32C states keep no ghost cells: every reader maps them on the fly
+  if (s->fp32) return E2D_OK;
   E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_GHOSTS_IN, s->stream), "make_boundaries");
   return E2D_OK;
 }
@@ -363,11 +423,12 @@ int e2d_make_boundaries(e2d_sim *s, int which) {
 int e2d_compute_dt(e2d_sim *s, int useU, double *dt) {
   if (!s || !dt) return set_err(s, E2D_EINVAL, "bad compute_dt args");
   const int which = (useU == 0) ? 0 : 1;
-  s->clk_host->invdt_bits = 0ull;
-  s->clk_host->status = 0u;
   E2D_CK(s, cudaMemsetAsync(&s->clk->invdt_bits, 0, sizeof(unsigned long long), s->stream), "dt reset");
   E2D_CK(s, cudaMemsetAsync(&s->clk->status, 0, sizeof(unsigned int), s->stream), "dt reset");
-  E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_DT, s->stream), "compute_dt");
+  if (s->fp32)
+    E2D_CK(s, launch_f32c_dt(s->kp32, s->W[which], s->clk, -1, s->stream), "compute_dt");
+  else
+    E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_DT, s->stream), "compute_dt");
   E2D_CK(s, cudaMemcpyAsync(s->clk_host, s->clk, sizeof(DevClock), cudaMemcpyDeviceToHost, s->stream), "dt copy");
   E2D_CK(s, cudaStreamSynchronize(s->stream), "dt sync");
   double inv;
@@ -380,6 +441,11 @@ int e2d_compute_dt(e2d_sim *s, int useU, double *dt) {
 int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   if (!s) return E2D_EINVAL;
   const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
+  if (s->fp32) {
+    E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 0, dt,
+                               nullptr, s->stream), "godunov step");
+    return E2D_OK;
+  }
   double *in = s->U[par], *out = s->U[par ^ 1];
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT;
   E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream), "godunov primitives");
@@ -402,17 +468,25 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   *s->clk_host = c;
   E2D_CK(s, cudaMemcpyAsync(s->clk, s->clk_host, sizeof(DevClock), cudaMemcpyHostToDevice, s->stream), "clock upload");
   const int par0 = (*nStep % 2 == 0) ? 0 : 1;
+  // FP32C: the first step's CFL maximum; later steps fold it in their epilogue
+  if (s->fp32) E2D_CK(s, launch_f32c_dt(s->kp32, s->W[par0], s->clk, *nStep & 1, s->stream), "initial dt");
   if (s->profiling) {
     size_t ev = 0;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
-    const char *rs = s->p.riemannSolverType == E2D_RIEMANN_HLLC ? "hllc"
-                     : s->p.riemannSolverType == E2D_RIEMANN_HLL ? "hll" : "approx";
-    const std::string k2 = std::string("k_flux_update_f64<") + rs + ">";
+    const std::string rs = riemann_name(s->p.riemannSolverType);
     for (int k = 0; k < n; ++k) {
       const int par = (par0 + k) & 1;
-      double *in = s->U[par], *out = s->U[par ^ 1];
       cudaEvent_t a = pool_event(s, ev++), b = pool_event(s, ev++), c2 = pool_event(s, ev++);
       if (!a || !b || !c2) return set_err(s, E2D_ECUDA, "event create");
+      if (s->fp32) {
+        E2D_CK(s, cudaEventRecord(a, s->stream), "event");
+        E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1, 0.0,
+                                   s->dt_trace, s->stream), "step");
+        E2D_CK(s, cudaEventRecord(b, s->stream), "event");
+        marks.push_back({"k_step_f32c<" + rs + ">", {a, b}});
+        continue;
+      }
+      double *in = s->U[par], *out = s->U[par ^ 1];
       E2D_CK(s, cudaEventRecord(a, s->stream), "event");
       E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk,
                                 FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK,
@@ -422,15 +496,13 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
                                        s->dt_trace, s->stream), "flux");
       E2D_CK(s, cudaEventRecord(c2, s->stream), "event");
       marks.push_back({"k_fill_f64", {a, b}});
-      marks.push_back({k2, {b, c2}});
+      marks.push_back({"k_flux_update_f64<" + rs + ">", {b, c2}});
     }
     E2D_CK(s, cudaStreamSynchronize(s->stream), "profiled step sync");
     for (auto &m : marks) {
       float ms = 0.f;
       E2D_CK(s, cudaEventElapsedTime(&ms, m.second.first, m.second.second), "event time");
-      if (!s->k_count.count(m.first)) s->k_names.push_back(m.first);
-      s->k_ms[m.first] += ms;
-      s->k_count[m.first] += 1;
+      record_kernel(s, m.first, ms);
     }
   } else {
     int done = 0;
@@ -453,6 +525,38 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   if (s->clk_host->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT))
     return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
                                                                               : "non-positive or non-finite dt");
+  return E2D_OK;
+}
+
+int e2d_conservation(e2d_sim *s, int which, double sums[4]) {
+  if (!s || !sums || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad conservation args");
+  double *u = nullptr;
+  int rc = fp64_view(s, which, &u);
+  if (rc != E2D_OK) return rc;
+  E2D_CK(s, launch_sums_f64(s->kp.g, u, s->partial, s->red_out, s->stream), "conservation");
+  E2D_CK(s, cudaMemcpyAsync(sums, s->red_out, sizeof(double) * 4, cudaMemcpyDeviceToHost, s->stream), "conservation copy");
+  E2D_CK(s, cudaStreamSynchronize(s->stream), "conservation sync");
+  return E2D_OK;
+}
+
+int e2d_l1_diff(e2d_sim *a, int wa, e2d_sim *b, int wb, int var, double *l1_diff, double *l1_ref) {
+  if (!a || !b || !l1_diff || !l1_ref || var < 0 || var > 3 || (wa != 0 && wa != 1) || (wb != 0 && wb != 1))
+    return set_err(a, E2D_EINVAL, "bad l1_diff args");
+  if (a->p.nx != b->p.nx || a->p.ny != b->p.ny) return set_err(a, E2D_EINVAL, "l1_diff: grids differ");
+  if (a == b && a->fp32) return set_err(a, E2D_EINVAL, "l1_diff: one FP32C handle has one staging array");
+  double *ua = nullptr, *ub = nullptr;
+  int rc = fp64_view(a, wa, &ua);
+  if (rc != E2D_OK) return rc;
+  E2D_CK(a, cudaStreamSynchronize(a->stream), "l1 sync");
+  rc = fp64_view(b, wb, &ub);
+  if (rc != E2D_OK) return rc;
+  E2D_CK(b, cudaStreamSynchronize(b->stream), "l1 sync");
+  E2D_CK(a, launch_l1diff_f64(a->kp.g, ua, ub, var, a->partial, a->red_out, a->stream), "l1_diff");
+  double r[2];
+  E2D_CK(a, cudaMemcpyAsync(r, a->red_out, sizeof(r), cudaMemcpyDeviceToHost, a->stream), "l1 copy");
+  E2D_CK(a, cudaStreamSynchronize(a->stream), "l1 sync");
+  *l1_diff = r[0];
+  *l1_ref = r[1];
   return E2D_OK;
 }
 

@@ -143,12 +143,23 @@ int e2d_get_state(e2d_sim *sim, int which, double *host, int layout);
  * or U2 (1) and an ASCII VTK ImageData (.vti) file of the interior cells,
  * variables rho, E, mx, my in the reference's text format. */
 int e2d_save_vtk(e2d_sim *sim, int which, const char *filename);
-/* Device address of U (which = 0) or U2 (1), LayoutLeft, for zero-copy use. */
+/* Device address of U (which = 0) or U2 (1), LayoutLeft FP64, for zero-copy
+ * use.  FP32C handles return a converted copy (hi + lo, ghosts filled) in a
+ * staging array that the next call on the handle may overwrite. */
 int e2d_device_state(e2d_sim *sim, int which, double **dptr);
+/* Conservation audit: FP64 sums over the interior cells of rho, E, mx, my of
+ * U (0) or U2 (1); deterministic summation order. */
+int e2d_conservation(e2d_sim *sim, int which, double sums[4]);
+/* L1 difference of variable var between state wa of a and state wb of b
+ * (same grid): *l1_diff = sum |a - b|, *l1_ref = sum |b| over the interior,
+ * accumulated in FP64 on the device of a. */
+int e2d_l1_diff(e2d_sim *a, int wa, e2d_sim *b, int wb, int var, double *l1_diff, double *l1_ref);
 /* The handle's CUDA stream (a cudaStream_t). */
 int e2d_get_stream(e2d_sim *sim, void **stream);
 
-/* HydroRun::make_boundaries (src/HydroRun.h:388-399) on U (0) or U2 (1). */
+/* HydroRun::make_boundaries (src/HydroRun.h:388-399) on U (0) or U2 (1).
+ * FP32C states keep no ghost cells (readers map them), so there it does
+ * nothing. */
 int e2d_make_boundaries(e2d_sim *sim, int which);
 /* HydroRun::compute_dt (src/HydroRun.h:227-251): cfl / max wave speed of U
  * (useU == 0) or U2; blocks until the value is on the host. */

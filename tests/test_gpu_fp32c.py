@@ -1,0 +1,110 @@
+"""The FP32 path with compensated (hi, lo) update against the FP64 path.
+
+Tolerances (relative L1 of density over the interior, FP64 accumulation):
+FP32C_L1_TOL below.  The FP64 path is itself bit-identical to the reference
+(test_gpu_parity.py), so it is the oracle here."""
+import numpy as np
+import pytest
+
+import _cases as C
+import euler2d_kokkos_gb300 as e2d
+
+pytestmark = pytest.mark.gpu
+
+FP32C_L1_TOL = 1e-5
+
+
+def pair(text, tmp_path, u0=None, riemann=None):
+    p64 = e2d.HydroParams.from_ini(C.write_ini(text, str(tmp_path), "a.ini"))
+    if riemann:
+        p64.riemannSolverType = e2d.RIEMANN[riemann]
+    p32 = p64.copy()
+    p32.precision = e2d.PRECISION_FP32C
+    h64 = e2d.HydroRun(p64.init())
+    h32 = e2d.HydroRun(p32.init())
+    if u0 is not None:
+        for h in (h64, h32):
+            h.set_state(0, u0)
+            h.set_state(1, u0)
+    return h64, h32
+
+
+def rel_l1(h32, w32, h64, w64, var=0):
+    d, r = h32.l1_diff(w32, h64, w64, var)
+    return d / r
+
+
+@pytest.mark.parametrize("case,nsteps", [("implode_diag", 100), ("blast_reflect", 60),
+                                         ("four_quadrant_absorb", 60), ("periodic_smooth", 50),
+                                         ("mixed_bc_smooth", 40)])
+def test_fp32c_close_to_fp64(gpu_lib, runs, tmp_path, case, nsteps):
+    text = str(runs[f"{case}__ini"])
+    h64, h32 = pair(text, tmp_path, runs[f"{case}__u0"])
+    t64, n64, dt64 = h64.step_n(nsteps, 10.0, 0.0, 0)
+    t32, n32, dt32 = h32.step_n(nsteps, 10.0, 0.0, 0)
+    assert n64 == n32 == nsteps
+    assert np.allclose(dt32, dt64, rtol=1e-5, atol=0)
+    # fixed-time comparison: both runs end at nearly the same time
+    err = rel_l1(h32, n32 % 2, h64, n64 % 2)
+    assert err < FP32C_L1_TOL, err
+    # the FP64 path matches the reference bit for bit
+    assert np.array_equal(h64.current(n64), runs[f"{case}__u"])
+
+
+def test_fp32c_initial_conditions_equal_fp64(gpu_lib, tmp_path):
+    text = C.ini_text(64, 48, problem="four_quadrant", bc=(2, 2, 2, 2))
+    h64, h32 = pair(text, tmp_path)
+    u64, u32 = h64.U, h32.U
+    # hi + lo represents every FP64 initial value to ~2^-48 relative
+    assert np.allclose(u32, u64, rtol=2e-14, atol=0)
+
+
+def test_fp32c_mass_conserved_periodic(gpu_lib, tmp_path):
+    """Every face flux is added to one cell and subtracted from its neighbour
+    with compensated sums: total mass/momentum/energy drift stays at FP64
+    round-off level on a periodic domain."""
+    text = C.ini_text(96, 80, bc=(3, 3, 3, 3))
+    u0 = C.smooth_state(96, 80, C.f32(1.4), seed=21)
+    _, h32 = pair(text, tmp_path, u0)
+    s0 = h32.conservation(0)
+    t, ns, _ = h32.step_n(200, 10.0, 0.0, 0)
+    s1 = h32.conservation(ns % 2)
+    rel = np.abs(s1 - s0) / np.abs(s0).clip(1e-300)
+    assert rel[0] < 1e-10 and rel[1] < 1e-10, rel
+
+
+@pytest.mark.parametrize("riemann", ["hll", "approx"])
+def test_fp32c_other_solvers(gpu_lib, runs, tmp_path, riemann):
+    case = "four_quadrant_absorb"
+    text = str(runs[f"{case}__ini"]).replace("riemann=hllc", f"riemann={riemann}")
+    h64, h32 = pair(text, tmp_path, runs[f"{case}__u0"])
+    _, n64, _ = h64.step_n(30, 10.0, 0.0, 0)
+    _, n32, _ = h32.step_n(30, 10.0, 0.0, 0)
+    assert rel_l1(h32, n32 % 2, h64, n64 % 2) < FP32C_L1_TOL
+
+
+def test_fp32c_host_loop_matches_device_loop(gpu_lib, runs, tmp_path):
+    case = "blast_reflect"
+    text = str(runs[f"{case}__ini"])
+    _, ha = pair(text, tmp_path, runs[f"{case}__u0"])
+    _, hb = pair(text, tmp_path, runs[f"{case}__u0"])
+    t, ns, dts = ha.step_n(40, 10.0, 0.0, 0)
+    tb, nb = 0.0, 0
+    for _ in range(40):
+        dt = hb.compute_dt(nb % 2)
+        hb.godunov_unsplit(nb, dt)
+        nb += 1
+        tb += dt
+    assert abs(tb - t) <= 1e-6 * t
+    assert rel_l1(hb, nb % 2, ha, ns % 2) < 1e-5
+
+
+def test_fp32c_conservation_audit_fp64_matches_numpy(gpu_lib, tmp_path):
+    text = C.ini_text(40, 30)
+    u0 = C.smooth_state(40, 30, C.f32(1.4), seed=5)
+    h64, _ = pair(text, tmp_path, u0)
+    s = h64.conservation(0)
+    inner = u0[:, 2:-2, 2:-2].reshape(4, -1)
+    ref = inner.sum(axis=1)
+    # summation order differs from numpy's: bound by the sum of magnitudes
+    assert np.all(np.abs(s - ref) <= 1e-13 * np.abs(inner).sum(axis=1)), (s, ref)
