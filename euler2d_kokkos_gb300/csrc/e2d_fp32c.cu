@@ -321,19 +321,35 @@ __global__ void __launch_bounds__(NT, 4)
   const int tid = threadIdx.x;
   const long long P = g.plane;
 
-  double dt = host_dt, t = 0.0;
-  int slot = 0;
-  if (use_clock) {
-    t = clk->t;
-    const double t_end = clk->t_end;
-    if (!(t < t_end)) return;
-    slot = clk->nstep & 1;
-    const double inv_dt = __longlong_as_double((long long)clk->acc[slot]);
-    dt = kp.ph64.cfl / inv_dt;
-    if (t + dt > t_end) dt = t_end - t;
+  // dt of this step (FP64, src/main.cpp:128-134), computed by one thread: the
+  // FP64 pipe runs at 1/70 of the FP32 rate, so per-thread divisions here
+  // would dominate the kernel
+  __shared__ double s_dt[3];
+  __shared__ int s_run, s_slot;
+  if (tid == 0) {
+    double dt = host_dt, t = 0.0;
+    int run = 1, slot = 0;
+    if (use_clock) {
+      t = clk->t;
+      const double t_end = clk->t_end;
+      run = t < t_end;
+      slot = clk->nstep & 1;
+      const double inv_dt = __longlong_as_double((long long)clk->acc[slot]);
+      dt = kp.ph64.cfl / inv_dt;
+      if (t + dt > t_end) dt = t_end - t;
+    }
+    s_dt[0] = dt;
+    s_dt[1] = dt / kp.ph64.dx;
+    s_dt[2] = dt / kp.ph64.dy;
+    s_run = run;
+    s_slot = slot;
   }
-  const float dtdx = (float)(dt / kp.ph64.dx);
-  const float dtdy = (float)(dt / kp.ph64.dy);
+  __syncthreads();
+  if (!s_run) return;
+  const double dt = s_dt[0];
+  const int slot = s_slot;
+  const float dtdx = (float)s_dt[1];
+  const float dtdy = (float)s_dt[2];
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
 
   // stage 1: primitives of the tile and its halo; ghosts via the boundary map
@@ -487,7 +503,7 @@ __global__ void __launch_bounds__(NT, 4)
       if (dt_trace && tslot >= 0 && tslot < clk->trace_cap) dt_trace[tslot] = dt;
       if (!(dt > 0.0) || nonfinite64(dt)) clk->status |= E2D_FLAG_BAD_DT;
       clk->dt = dt;
-      clk->t = t + dt;
+      clk->t = clk->t + dt;  // only this block writes t during the step
       clk->nstep = ns + 1;
       clk->acc[slot] = 0ull;
       clk->done_blocks = 0u;

@@ -386,17 +386,32 @@ __global__ void __launch_bounds__(NT, 2)
   const int tid = threadIdx.x;
 
   // dt of this step: the caller's, or src/main.cpp:128-134 on the device
-  double dt = host_dt, t = 0.0;
-  if (use_clock) {
-    t = clk->t;
-    const double t_end = clk->t_end;
-    if (!(t < t_end)) return;
-    const double inv_dt = __longlong_as_double((long long)clk->invdt_bits);
-    dt = ph.cfl / inv_dt;
-    if (t + dt > t_end) dt = t_end - t;
+  // dt of this step (src/main.cpp:128-134 on the device) and dt/dx, dt/dy,
+  // computed once per block and broadcast: per-thread FP64 divisions here
+  // would cost ~2 divisions per cell on the FP64 pipe
+  __shared__ double s_dt[3];
+  __shared__ int s_run;
+  if (tid == 0) {
+    double dt = host_dt;
+    int run = 1;
+    if (use_clock) {
+      const double t = clk->t;
+      const double t_end = clk->t_end;
+      run = t < t_end;
+      const double inv_dt = __longlong_as_double((long long)clk->invdt_bits);
+      dt = ph.cfl / inv_dt;
+      if (t + dt > t_end) dt = t_end - t;
+    }
+    s_dt[0] = dt;
+    s_dt[1] = dt / ph.dx;
+    s_dt[2] = dt / ph.dy;
+    s_run = run;
   }
-  const double dtdx = dt / ph.dx;
-  const double dtdy = dt / ph.dy;
+  __syncthreads();
+  if (!s_run) return;
+  const double dt = s_dt[0];
+  const double dtdx = s_dt[1];
+  const double dtdy = s_dt[2];
 
   const int i0 = blockIdx.x * TX;  // array column of the tile's first halo cell
   const int j0 = blockIdx.y * TY;
@@ -529,7 +544,7 @@ __global__ void __launch_bounds__(NT, 2)
       if (dt_trace && slot >= 0 && slot < clk->trace_cap) dt_trace[slot] = dt;
       if (!(dt > 0.0) || nonfinite(dt)) clk->status |= E2D_FLAG_BAD_DT;
       clk->dt = dt;
-      clk->t = t + dt;
+      clk->t = clk->t + dt;  // only this block writes t during the step
       clk->nstep = ns + 1;
       clk->invdt_bits = 0ull;
       clk->done_blocks = 0u;
