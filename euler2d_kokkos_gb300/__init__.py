@@ -110,6 +110,7 @@ SIGNATURES = {
     "e2d_make_boundaries": ([_V, _I], _I),
     "e2d_compute_dt": ([_V, _I, ctypes.POINTER(_D)], _I),
     "e2d_godunov_unsplit": ([_V, _I, _D], _I),
+    "e2d_godunov_unsplit_noalloc": ([_P, _V, _V, _D, _V], _I),
     "e2d_step_n": ([_V, _I, _D, ctypes.POINTER(_D), ctypes.POINTER(_I), _V], _I),
     "e2d_eval_device": ([_P, _I, _I, _V, _V, _D, _D], _I),
     "e2d_conservation": ([_V, _I, _V], _I),

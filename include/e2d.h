@@ -168,6 +168,30 @@ int e2d_compute_dt(e2d_sim *sim, int useU, double *dt);
  * nStep, U2 -> U for odd, with the caller's dt.  Asynchronous. */
 int e2d_godunov_unsplit(e2d_sim *sim, int nStep, double dt);
 
+/* One FP64 godunov_unsplit step (same kernels and bits as
+ * e2d_godunov_unsplit) on device buffers the caller owns, allocating no
+ * memory at all.  No counterpart in the reference: it exists for callers
+ * that cannot let a library call cudaMalloc -- hosts that give out all
+ * device memory from their own fixed pool, latency-critical loops that
+ * cannot afford cudaMalloc's implicit device synchronisation, and code that
+ * keeps no handle between calls.
+ *   u_in, u_out: distinct device arrays of 4*isize*jsize doubles (LayoutLeft);
+ *   like the reference, the ghost cells of u_in are filled in place and u_out
+ *   receives the whole new state.  stream: a cudaStream_t, or NULL.  The call
+ *   is asynchronous on that stream.
+ * Scratch (primitives and loop state) lives in one file-scope device array
+ * sized for E2D_NOALLOC_MAX_CELLS cells (isize*jsize, ghosts included):
+ * larger grids are refused with E2D_EINVAL.  Each GPU that loads the library
+ * holds that array (about 8.4 MB) until the process exits.  The first call
+ * on a device looks up the array's device address (and sets the kernels'
+ * shared-memory limit) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the one array, so
+ * calls that overlap on the GPU (different streams, or host threads without
+ * ordering) race with each other; serialise them.  FP64 precision only. */
+#define E2D_NOALLOC_MAX_CELLS (1 << 18)
+int e2d_godunov_unsplit_noalloc(const e2d_params *p, double *u_in, double *u_out, double dt,
+                                void *stream);
+
 /* The time loop of src/main.cpp:100-145 for up to n steps on the device:
  * each step takes dt = cfl/max wave speed of the current state, clamps it to
  * t_end - t, runs godunov_unsplit and advances (t, nStep); steps with
