@@ -4,6 +4,7 @@
 #include "e2d_internal.h"
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -114,7 +115,7 @@ const char *riemann_name(int r) {
 cudaError_t enqueue_step(e2d_sim *s, int par) {
   if (s->fp32)
     return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1,
-                            0.0, s->dt_trace, s->stream);
+                            0.0, s->stream);
   double *in = s->U[par], *out = s->U[par ^ 1];
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK;
   cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream);
@@ -251,6 +252,8 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
   s->fp32 = (p.precision == E2D_PRECISION_FP32C) ? 1 : 0;
   make_kparams(p, &s->kp);
   make_kparams32(p, &s->kp32);
+  if (const char *v = std::getenv("E2D_F32C_VARIANT")) s->kp32.variant = std::atoi(v);
+  if (const char *v = std::getenv("E2D_F32C_STRIP_H")) s->kp32.strip_h = std::atoi(v) > 0 ? std::atoi(v) : s->kp32.strip_h;
   auto fail = [&](int status) {
     e2d_destroy(s);
     return status;
@@ -260,9 +263,10 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(E2D_ECUDA);
   const size_t n = cells(s);
   if (s->fp32) {
+    const size_t wn = (size_t)8 * s->kp32.wplane;
     for (int k = 0; k < 2; ++k) {
-      if (cudaMalloc(&s->W[k], sizeof(float) * 8 * n) != cudaSuccess) return fail(E2D_ENOMEM);
-      if (cudaMemsetAsync(s->W[k], 0, sizeof(float) * 8 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+      if (cudaMalloc(&s->W[k], sizeof(float) * wn) != cudaSuccess) return fail(E2D_ENOMEM);
+      if (cudaMemsetAsync(s->W[k], 0, sizeof(float) * wn, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
     }
     if (cudaMalloc(&s->stage, sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
   } else {
@@ -333,7 +337,7 @@ int e2d_init_problem(e2d_sim *s) {
   if (s->fp32) {
     E2D_CK(s, launch_init_f64(s->kp, s->p, s->stage, s->stream), "init problem");
     E2D_CK(s, launch_f32c_from_f64(s->kp32, s->stage, s->W[0], s->stream), "init convert");
-    E2D_CK(s, cudaMemcpyAsync(s->W[1], s->W[0], sizeof(float) * 8 * cells(s), cudaMemcpyDeviceToDevice, s->stream), "init copy");
+    E2D_CK(s, cudaMemcpyAsync(s->W[1], s->W[0], sizeof(float) * 8 * s->kp32.wplane, cudaMemcpyDeviceToDevice, s->stream), "init copy");
   } else {
     E2D_CK(s, launch_init_f64(s->kp, s->p, s->U[0], s->stream), "init problem");
     E2D_CK(s, cudaMemcpyAsync(s->U[1], s->U[0], sizeof(double) * 4 * cells(s), cudaMemcpyDeviceToDevice, s->stream), "init copy");
@@ -443,7 +447,7 @@ int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
   if (s->fp32) {
     E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 0, dt,
-                               nullptr, s->stream), "godunov step");
+                               s->stream), "godunov step");
     return E2D_OK;
   }
   double *in = s->U[par], *out = s->U[par ^ 1];
@@ -465,6 +469,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   c.nstep = *nStep;
   c.trace_base = *nStep;
   c.trace_cap = n;
+  c.trace = s->dt_trace;
   *s->clk_host = c;
   E2D_CK(s, cudaMemcpyAsync(s->clk, s->clk_host, sizeof(DevClock), cudaMemcpyHostToDevice, s->stream), "clock upload");
   const int par0 = (*nStep % 2 == 0) ? 0 : 1;
@@ -481,7 +486,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
       if (s->fp32) {
         E2D_CK(s, cudaEventRecord(a, s->stream), "event");
         E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1, 0.0,
-                                   s->dt_trace, s->stream), "step");
+                                   s->stream), "step");
         E2D_CK(s, cudaEventRecord(b, s->stream), "event");
         marks.push_back({"k_step_f32c<" + rs + ">", {a, b}});
         continue;

@@ -5,15 +5,21 @@
 // are not rounded away; slopes, traces and Riemann fluxes are computed in FP32
 // from hi.  The update adds the flux balance with TwoSum (Knuth, "The Art of
 // Computer Programming" vol. 2, 4.2.2) and renormalises with Fast2Sum
-// (Dekker, 1971).  The CFL maximum stays FP64: each block selects its
-// largest FP32 wave-speed term and recomputes that cell's term in FP64 from
-// hi + lo; blocks combine with an FP64 max.
+// (Dekker, 1971).  The CFL maximum stays FP64: each warp selects its largest
+// FP32 wave-speed term and, unless it is clearly below the running maximum,
+// recomputes that cell's term in FP64 from hi + lo; warps combine with an
+// FP64 max.
 //
-// One launch per time step (k_step_f32c): per 32x16 tile it reads hi of the
-// tile and its 2-cell halo (ghost cells through the boundary map, so no fill
-// pass), computes primitives, slopes, face states and fluxes in shared
-// memory, writes the updated (hi, lo) and folds the next step's CFL maximum
-// into the device clock.  Algorithmic traffic: 32 B read + 32 B written per
+// k_step_f32c -- one launch per time step, a register march: each lane owns
+// two adjacent columns, each warp a strip of 60 output columns (64 loaded:
+// the 2-column halo on each side) by strip_h rows, and walks down the strip one row
+// at a time keeping three rows of primitives, the previous row's face states
+// and fluxes in registers.  Neighbour columns come from warp shuffles; there
+// is no shared-memory staging and no block barrier in the march.  The two
+// columns of a lane are computed together with Blackwell's packed FP32
+// instructions (FFMA2 / FADD2 / FMUL2 on float2).  Ghost cells are read
+// through the boundary map, so no fill pass runs and ghost cells of the
+// arrays are never read.  Algorithmic traffic: 32 B read + 32 B written per
 // cell.
 #include "e2d_common.cuh"
 #include "e2d_internal.h"
@@ -21,125 +27,147 @@
 namespace e2d {
 namespace {
 
-constexpr int TX = 32;
-constexpr int TY = 16;
-constexpr int QW = TX + 4;
-constexpr int QH = TY + 4;
-constexpr int XW = TX + 2;
-constexpr int YH = TY + 2;
-constexpr int NT = 256;
-constexpr size_t kSmemFloats = 4 * QH * QW + 2 * (4 * TY * XW) + 2 * (4 * YH * TX);
+constexpr int LANES = 32;
+constexpr int OUTW = 60;   // output columns per warp strip (lanes 1..30)
+constexpr int WPB = 4;     // warps (strips) per block
+constexpr int NT = WPB * LANES;
 
-// ------------------------------------------------------------ FP32 numerics
-// Same equations as the FP64 path (src/HydroBaseFunctor.h), FP32 arithmetic.
-__device__ __forceinline__ void prims32(const KPhys<float> &ph, float rho, float e, float mx, float my,
-                                        float &d, float &p, float &ux, float &uy) {
-  d = fmaxf(rho, ph.smallr);
-  const float inv = 1.0f / d;
-  ux = mx * inv;
-  uy = my * inv;
-  const float eken = 0.5f * (ux * ux + uy * uy);
-  const float ei = e * inv - eken;
-  p = fmaxf(ph.gm1 * d * ei, d * ph.smallp);
+// ------------------------------------------------------------ packed FP32
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) {
+  return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);  // a + (-1)*b: one rounding, = a - b
+}
+__device__ __forceinline__ float2 operator*(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 max2(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
+__device__ __forceinline__ float2 min2(float2 a, float2 b) { return make_float2(fminf(a.x, b.x), fminf(a.y, b.y)); }
+__device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(1.0f / a.x, 1.0f / a.y); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
+__device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
+  return make_float2(cx ? a.x : b.x, cy ? a.y : b.y);
 }
 
-__device__ __forceinline__ float slope32(int st_kind, float st, float q, float qp, float qm) {
-  if (st_kind == 0) return 0.0f;
-  const float dlft = st * (q - qm);
-  const float drgt = st * (qp - q);
-  const float dcen = 0.5f * (qp - qm);
-  const float slop = fminf(fabsf(dlft), fabsf(drgt));
-  const float dlim = (dlft * drgt <= 0.0f) ? 0.0f : slop;
-  const float m = fminf(dlim, fabsf(dcen));
-  return dcen >= 0.0f ? m : -m;
+// Constants broadcast to both halves of a float2.
+struct C2 {
+  float2 half, smallr, smallp, smallc2, gamma0, gm1, entho, st;
+};
+
+__device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
+  C2 k;
+  k.half = f2(0.5f);
+  k.smallr = f2(ph.smallr);
+  k.smallp = f2(ph.smallp);
+  k.smallc2 = f2(ph.smallc2);
+  k.gamma0 = f2(ph.gamma0);
+  k.gm1 = f2(ph.gm1);
+  k.entho = f2(ph.entho);
+  k.st = f2(ph.slope_type);
+  return k;
 }
 
-__device__ __forceinline__ void sources32(const KPhys<float> &ph, const float q[4], const float dqx[4],
-                                          const float dqy[4], float s0[4]) {
-  const float r = q[E2D_ID], p = q[E2D_IP], u = q[E2D_IU], v = q[E2D_IV];
-  const float ir = 1.0f / r;
-  const float div = dqx[E2D_IU] + dqy[E2D_IV];
-  s0[E2D_ID] = -u * dqx[E2D_ID] - v * dqy[E2D_ID] - div * r;
-  s0[E2D_IP] = -u * dqx[E2D_IP] - v * dqy[E2D_IP] - div * ph.gamma0 * p;
-  s0[E2D_IU] = -u * dqx[E2D_IU] - v * dqy[E2D_IU] - dqx[E2D_IP] * ir;
-  s0[E2D_IV] = -u * dqx[E2D_IV] - v * dqy[E2D_IV] - dqy[E2D_IP] * ir;
+// computePrimitives (src/HydroBaseFunctor.h:76-102) for two cells.
+__device__ __forceinline__ void prims2(const C2 &k, float2 rho, float2 e, float2 mx, float2 my,
+                                       float2 q[4]) {
+  const float2 d = max2(rho, k.smallr);
+  const float2 inv = rcp2(d);
+  const float2 u = mx * inv, v = my * inv;
+  const float2 eken = k.half * fma2(u, u, v * v);
+  const float2 ei = fma2(e, inv, neg2(eken));
+  q[E2D_ID] = d;
+  q[E2D_IP] = max2(k.gm1 * d * ei, d * k.smallp);
+  q[E2D_IU] = u;
+  q[E2D_IV] = v;
 }
 
-__device__ __forceinline__ void riemann_hllc32(const KPhys<float> &ph, const float *ql, const float *qr,
-                                               float *flux) {
-  const float rl = fmaxf(ql[E2D_ID], ph.smallr);
-  const float pl = fmaxf(ql[E2D_IP], rl * ph.smallp);
-  const float ul = ql[E2D_IU], vl = ql[E2D_IV];
-  const float rr = fmaxf(qr[E2D_ID], ph.smallr);
-  const float pr = fmaxf(qr[E2D_IP], rr * ph.smallp);
-  const float ur = qr[E2D_IU], vr = qr[E2D_IV];
-  const float etotl = pl * ph.entho + 0.5f * rl * (ul * ul + vl * vl);
-  const float etotr = pr * ph.entho + 0.5f * rr * (ur * ur + vr * vr);
-  const float cfastl = sqrtf(fmaxf(ph.gamma0 * pl / rl, ph.smallc2));
-  const float cfastr = sqrtf(fmaxf(ph.gamma0 * pr / rr, ph.smallc2));
-  const float cmax = fmaxf(cfastl, cfastr);
-  const float SL = fminf(ul, ur) - cmax;
-  const float SR = fmaxf(ul, ur) + cmax;
-  const float rcl = rl * (ul - SL);
-  const float rcr = rr * (SR - ur);
-  const float iden = 1.0f / (rcr + rcl);
-  const float ustar = (rcr * ur + rcl * ul + (pl - pr)) * iden;
-  const float ptotstar = (rcr * pl + rcl * pr + rcl * rcr * (ul - ur)) * iden;
-  const bool lft = ustar > 0.0f;
-  const float S = lft ? SL : SR;
-  const float rs = lft ? rl : rr, us = lft ? ul : ur, ps = lft ? pl : pr, es = lft ? etotl : etotr;
-  const float sdu = S - us;
-  const float isds = 1.0f / (S - ustar);
-  const float rstar = rs * sdu * isds;
-  const float etotstar = (sdu * es - ps * us + ptotstar * ustar) * isds;
-  float ro, uo, ptoto, etoto;
-  if (SL > 0.0f) {
-    ro = rl, uo = ul, ptoto = pl, etoto = etotl;
-  } else if (lft || SR > 0.0f) {
-    ro = rstar, uo = ustar, ptoto = ptotstar, etoto = etotstar;
-  } else {
-    ro = rr, uo = ur, ptoto = pr, etoto = etotr;
+// slope_unsplit_hydro_2d_scalar (src/HydroBaseFunctor.h:421-455), one
+// direction, two cells; slope_type 0 is handled by the caller.  The
+// reference's form -- zero when (q-qm)*(qp-q) <= 0, else
+// sign(dcen) * min(st|q-qm|, st|qp-q|, |dcen|) -- is evaluated as
+// s * max(0, min(st * min(s*(q-qm), s*(qp-q)), |dcen|)) with s = sign(dcen):
+// both one-sided differences share the sign of dcen exactly when their
+// product is positive, and a difference of the other sign makes the inner
+// minimum negative.
+__device__ __forceinline__ float2 slope2(const C2 &k, float2 q, float2 qp, float2 qm) {
+  const float2 dl = q - qm;
+  const float2 dr = qp - q;
+  const float2 dcen = k.half * (qp - qm);
+  const float2 s = make_float2(copysignf(1.0f, dcen.x), copysignf(1.0f, dcen.y));
+  const float2 lim = k.st * min2(s * dl, s * dr);
+  return s * max2(min2(lim, abs2(dcen)), f2(0.0f));
+}
+
+// riemann_hllc (src/HydroBaseFunctor.h:704-809) for two faces.
+__device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const float2 qr[4], float2 f[4]) {
+  const float2 rl = max2(ql[E2D_ID], k.smallr), rr = max2(qr[E2D_ID], k.smallr);
+  const float2 pl = max2(ql[E2D_IP], rl * k.smallp), pr = max2(qr[E2D_IP], rr * k.smallp);
+  const float2 ul = ql[E2D_IU], ur = qr[E2D_IU], vl = ql[E2D_IV], vr = qr[E2D_IV];
+  const float2 etotl = fma2(pl, k.entho, k.half * rl * fma2(ul, ul, vl * vl));
+  const float2 etotr = fma2(pr, k.entho, k.half * rr * fma2(ur, ur, vr * vr));
+  const float2 cl = sqrt2(max2(k.gamma0 * pl * rcp2(rl), k.smallc2));
+  const float2 cr = sqrt2(max2(k.gamma0 * pr * rcp2(rr), k.smallc2));
+  const float2 cmax = max2(cl, cr);
+  const float2 SL = min2(ul, ur) - cmax;
+  const float2 SR = max2(ul, ur) + cmax;
+  const float2 rcl = rl * (ul - SL);
+  const float2 rcr = rr * (SR - ur);
+  const float2 iden = rcp2(rcr + rcl);
+  const float2 ustar = fma2(rcr, ur, fma2(rcl, ul, pl - pr)) * iden;
+  const float2 ptotstar = fma2(rcr, pl, fma2(rcl, pr, rcl * rcr * (ul - ur))) * iden;
+  const bool lx = ustar.x > 0.0f, ly = ustar.y > 0.0f;
+  const float2 S = sel2(lx, ly, SL, SR);
+  const float2 rs = sel2(lx, ly, rl, rr), us = sel2(lx, ly, ul, ur), ps = sel2(lx, ly, pl, pr);
+  const float2 es = sel2(lx, ly, etotl, etotr);
+  const float2 sdu = S - us;
+  const float2 isds = rcp2(S - ustar);
+  const float2 rstar = rs * sdu * isds;
+  const float2 etotstar = fma2(ptotstar, ustar, fma2(sdu, es, neg2(ps * us))) * isds;
+  // SL > 0: left state; else star (left or right); SR <= 0: right state.
+  // Supersonic faces are rare: a warp with none of them skips the selects.
+  float2 ro = rstar, uo = ustar, po = ptotstar, eo = etotstar;
+  const bool sx = SL.x > 0.0f, sy = SL.y > 0.0f;
+  const bool tx = !sx && (lx || SR.x > 0.0f), ty = !sy && (ly || SR.y > 0.0f);
+  if (__any_sync(0xffffffffu, !(tx && ty))) {
+    ro = sel2(sx, sy, rl, sel2(tx, ty, rstar, rr));
+    uo = sel2(sx, sy, ul, sel2(tx, ty, ustar, ur));
+    po = sel2(sx, sy, pl, sel2(tx, ty, ptotstar, pr));
+    eo = sel2(sx, sy, etotl, sel2(tx, ty, etotstar, etotr));
   }
-  flux[E2D_ID] = ro * uo;
-  flux[E2D_IU] = flux[E2D_ID] * uo + ptoto;
-  flux[E2D_IP] = (etoto + ptoto) * uo;
-  flux[E2D_IV] = flux[E2D_ID] * (flux[E2D_ID] > 0.0f ? vl : vr);
+  f[E2D_ID] = ro * uo;
+  f[E2D_IU] = fma2(f[E2D_ID], uo, po);
+  f[E2D_IP] = (eo + po) * uo;
+  f[E2D_IV] = f[E2D_ID] * sel2(f[E2D_ID].x > 0.0f, f[E2D_ID].y > 0.0f, vl, vr);
 }
 
-__device__ __forceinline__ void riemann_hll32(const KPhys<float> &ph, const float *ql, const float *qr,
-                                              float *flux) {
-  const float rl = fmaxf(ql[E2D_ID], ph.smallr);
-  const float pl = fmaxf(ql[E2D_IP], rl * ph.smallp);
-  const float ul = ql[E2D_IU], vl = ql[E2D_IV];
-  const float rr = fmaxf(qr[E2D_ID], ph.smallr);
-  const float pr = fmaxf(qr[E2D_IP], rr * ph.smallp);
-  const float ur = qr[E2D_IU], vr = qr[E2D_IV];
-  const float etotl = pl * ph.entho + 0.5f * rl * (ul * ul + vl * vl);
-  const float etotr = pr * ph.entho + 0.5f * rr * (ur * ur + vr * vr);
-  const float cmax = fmaxf(sqrtf(fmaxf(ph.gamma0 * pl / rl, ph.smallc2)),
-                           sqrtf(fmaxf(ph.gamma0 * pr / rr, ph.smallc2)));
-  const float SL = fminf(ul, ur) - cmax;
-  const float SR = fmaxf(ul, ur) + cmax;
-  const float UL[4] = {rl, etotl, rl * ul, rl * vl};
-  const float UR[4] = {rr, etotr, rr * ur, rr * vr};
-  const float FL[4] = {UL[E2D_IU], (etotl + pl) * ul, UL[E2D_IU] * ul + pl, UL[E2D_IU] * vl};
-  const float FR[4] = {UR[E2D_IU], (etotr + pr) * ur, UR[E2D_IU] * ur + pr, UR[E2D_IU] * vr};
-  if (SL > 0.0f) {
+// HLL flux (Toro eq. 10.21, riemann_hllc's wave speeds) for two faces.
+__device__ __forceinline__ void hll2(const C2 &k, const float2 ql[4], const float2 qr[4], float2 f[4]) {
+  const float2 rl = max2(ql[E2D_ID], k.smallr), rr = max2(qr[E2D_ID], k.smallr);
+  const float2 pl = max2(ql[E2D_IP], rl * k.smallp), pr = max2(qr[E2D_IP], rr * k.smallp);
+  const float2 ul = ql[E2D_IU], ur = qr[E2D_IU], vl = ql[E2D_IV], vr = qr[E2D_IV];
+  const float2 etotl = fma2(pl, k.entho, k.half * rl * fma2(ul, ul, vl * vl));
+  const float2 etotr = fma2(pr, k.entho, k.half * rr * fma2(ur, ur, vr * vr));
+  const float2 cmax = max2(sqrt2(max2(k.gamma0 * pl * rcp2(rl), k.smallc2)),
+                           sqrt2(max2(k.gamma0 * pr * rcp2(rr), k.smallc2)));
+  const float2 SL = min2(ul, ur) - cmax;
+  const float2 SR = max2(ul, ur) + cmax;
+  const float2 UL[4] = {rl, etotl, rl * ul, rl * vl};
+  const float2 UR[4] = {rr, etotr, rr * ur, rr * vr};
+  const float2 FL[4] = {UL[E2D_IU], (etotl + pl) * ul, fma2(UL[E2D_IU], ul, pl), UL[E2D_IU] * vl};
+  const float2 FR[4] = {UR[E2D_IU], (etotr + pr) * ur, fma2(UR[E2D_IU], ur, pr), UR[E2D_IU] * vr};
+  const float2 iden = rcp2(SR - SL);
+  const float2 sls = SL * SR;
+  const bool ax = SL.x > 0.0f, ay = SL.y > 0.0f, bx = SR.x <= 0.0f, by = SR.y <= 0.0f;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = FL[v];
-  } else if (SR <= 0.0f) {
-#pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = FR[v];
-  } else {
-    const float iden = 1.0f / (SR - SL);
-    const float sls = SL * SR;
-#pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) * iden;
+  for (int v = 0; v < 4; ++v) {
+    const float2 mid = fma2(sls, UR[v] - UL[v], SR * FL[v] - SL * FR[v]) * iden;
+    f[v] = sel2(ax, ay, FL[v], sel2(bx, by, FR[v], mid));
   }
 }
 
-__device__ __noinline__ void riemann_approx32(const KPhys<float> &ph, const float *ql, const float *qr,
-                                              float *flux) {
+// riemann_approx (src/HydroBaseFunctor.h:558-693), one face, FP32.
+__device__ __noinline__ void approx1(const KPhys<float> &ph, const float *ql, const float *qr, float *flux) {
   const float gamma0 = ph.gamma0, gamma6 = ph.gamma6;
   const float rl = fmaxf(ql[E2D_ID], ph.smallr), ul = ql[E2D_IU];
   const float pl = fmaxf(ql[E2D_IP], rl * ph.smallp);
@@ -190,16 +218,26 @@ __device__ __noinline__ void riemann_approx32(const KPhys<float> &ph, const floa
 }
 
 template <int RS>
-__device__ __forceinline__ void riemann32(const KPhys<float> &ph, const float *ql, const float *qr, float *f) {
-  if (RS == E2D_RIEMANN_HLLC)
-    riemann_hllc32(ph, ql, qr, f);
-  else if (RS == E2D_RIEMANN_HLL)
-    riemann_hll32(ph, ql, qr, f);
-  else
-    riemann_approx32(ph, ql, qr, f);
+__device__ __forceinline__ void riemann2(const KPhys<float> &ph, const C2 &k, const float2 ql[4],
+                                         const float2 qr[4], float2 f[4]) {
+  if (RS == E2D_RIEMANN_HLLC) {
+    hllc2(k, ql, qr, f);
+  } else if (RS == E2D_RIEMANN_HLL) {
+    hll2(k, ql, qr, f);
+  } else {
+    float a[4], b[4], fa[4], fb[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) a[v] = ql[v].x, b[v] = qr[v].x;
+    approx1(ph, a, b, fa);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) a[v] = ql[v].y, b[v] = qr[v].y;
+    approx1(ph, a, b, fb);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) f[v] = make_float2(fa[v], fb[v]);
+  }
 }
 
-// CFL term of src/HydroRunFunctors.h:56-72 in FP64 from a compensated cell.
+// CFL term of src/HydroRunFunctors.h:56-72, FP64, from a compensated cell.
 __device__ __forceinline__ double cfl_term64(const KPhys<double> &ph, double rho, double e, double mx,
                                              double my) {
   const double d = fmax(rho, ph.smallr);
@@ -211,80 +249,84 @@ __device__ __forceinline__ double cfl_term64(const KPhys<double> &ph, double rho
   return (c + fabs(ux)) / ph.dx + (c + fabs(uy)) / ph.dy;
 }
 
+// The CFL term of two cells from their conserved values; idx = (1/dx, 1/dy).
+__device__ __forceinline__ float2 cfl_term2(const C2 &k, float2 idx, const float2 u[4]) {
+  float2 q[4];
+  prims2(k, u[0], u[1], u[2], u[3], q);
+  const float2 c = sqrt2(k.gamma0 * q[E2D_IP] * rcp2(q[E2D_ID]));
+  return fma2(c + abs2(q[E2D_IU]), f2(idx.x), (c + abs2(q[E2D_IV])) * f2(idx.y));
+}
+
 __device__ __forceinline__ float cfl_term32(const KPhys<float> &ph, float rho, float e, float mx, float my) {
-  float d, p, ux, uy;
-  prims32(ph, rho, e, mx, my, d, p, ux, uy);
-  const float c = sqrtf(ph.gamma0 * p / d);
+  const float d = fmaxf(rho, ph.smallr);
+  const float inv = 1.0f / d;
+  const float ux = mx * inv, uy = my * inv;
+  const float ei = e * inv - 0.5f * (ux * ux + uy * uy);
+  const float p = fmaxf(ph.gm1 * d * ei, d * ph.smallp);
+  const float c = sqrtf(ph.gamma0 * p * inv);
   return (c + fabsf(ux)) / ph.dx + (c + fabsf(uy)) / ph.dy;
 }
 
-// Block arg-max of an FP32 term; the winner's term is recomputed in FP64 from
-// its (hi, lo) state in w and folded into *target.  Every thread passes its
-// best (term, cell) pair; cell < 0 means none.
-__device__ __forceinline__ void block_cfl_fold(const KParams32 &kp, float term, int cell, const float *w,
-                                               unsigned long long *target, unsigned int *status) {
-  __shared__ float s_term[NT / 32];
-  __shared__ int s_cell[NT / 32];
+// Warp arg-max of an FP32 term, then lane 0 folds the winner's FP64 term
+// into *target -- skipped when the FP32 term is more than 1e-4 below the
+// running maximum (FP32 terms are within ~1e-6 of the FP64 ones, so such a
+// cell cannot raise the maximum).
+__device__ __forceinline__ void warp_cfl_fold(const KParams32 &kp, float term, long long cell,
+                                              const float *w, unsigned long long *target,
+                                              unsigned int *status) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     const float ot = __shfl_xor_sync(0xffffffffu, term, off);
-    const int oc = __shfl_xor_sync(0xffffffffu, cell, off);
+    const long long oc = __shfl_xor_sync(0xffffffffu, cell, off);
     if (ot > term || (ot == term && oc > cell)) term = ot, cell = oc;
   }
-  const int tid = threadIdx.x;
-  if ((tid & 31) == 0) {
-    s_term[tid >> 5] = term;
-    s_cell[tid >> 5] = cell;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    float bt = s_term[0];
-    int bc = s_cell[0];
-    for (int k = 1; k < NT / 32; ++k)
-      if (s_term[k] > bt || (s_term[k] == bt && s_cell[k] > bc)) bt = s_term[k], bc = s_cell[k];
-    if (bc >= 0) {
-      const long long P = kp.g.plane;
-      double u[4];
+  __syncwarp();  // the winner was written by a lane of this warp
+  if ((threadIdx.x & 31) != 0 || cell < 0) return;
+  const double cur = __longlong_as_double((long long)(*(volatile unsigned long long *)target));
+  if ((double)term < cur * (1.0 - 1e-4)) return;
+  const long long P = kp.wplane;
+  double u[4];
 #pragma unroll
-      for (int v = 0; v < 4; ++v) u[v] = (double)w[bc + v * P] + (double)w[bc + (4 + v) * P];
-      const double t64 = cfl_term64(kp.ph64, u[E2D_ID], u[E2D_IP], u[E2D_IU], u[E2D_IV]);
-      if (t64 > 0.0 && !nonfinite64(t64))
-        atomicMax(target, (unsigned long long)__double_as_longlong(t64));
-      else
-        atomicOr(status, nonfinite64(t64) ? (unsigned)E2D_FLAG_NONFINITE : (unsigned)E2D_FLAG_BAD_DT);
-    }
-  }
+  for (int v = 0; v < 4; ++v) u[v] = (double)w[cell + v * P] + (double)w[cell + (4 + v) * P];
+  const double t64 = cfl_term64(kp.ph64, u[E2D_ID], u[E2D_IP], u[E2D_IU], u[E2D_IV]);
+  if (t64 > 0.0 && !nonfinite64(t64))
+    atomicMax(target, (unsigned long long)__double_as_longlong(t64));
+  else
+    atomicOr(status, nonfinite64(t64) ? (unsigned)E2D_FLAG_NONFINITE : (unsigned)E2D_FLAG_BAD_DT);
 }
 
 // ------------------------------------------------------------ conversions
-__global__ void k_f32c_from_f64(const KGeom g, const double *__restrict__ u, float *__restrict__ w) {
-  const long long n = g.plane;
-  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+__global__ void k_f32c_from_f64(const KParams32 kp, const double *__restrict__ u, float *__restrict__ w) {
+  const KGeom &g = kp.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.isize || j >= g.jsize) return;
+  const long long s = i + (long long)g.isize * j, d = i + (long long)kp.wpitch * j;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const double x = u[k + v * n];
-      const float hi = (float)x;
-      w[k + v * n] = hi;
-      w[k + (4 + v) * n] = (float)(x - (double)hi);
-    }
+  for (int v = 0; v < 4; ++v) {
+    const double x = u[s + v * g.plane];
+    const float hi = (float)x;
+    w[d + v * kp.wplane] = hi;
+    w[d + (4 + v) * kp.wplane] = (float)(x - (double)hi);
   }
 }
 
 // hi + lo in FP64 for every cell; ghost cells through the boundary map (the
 // state after make_boundaries).
-__global__ void k_f32c_to_f64(const KGeom g, const float *__restrict__ w, double *__restrict__ u) {
+__global__ void k_f32c_to_f64(const KParams32 kp, const float *__restrict__ w, double *__restrict__ u) {
+  const KGeom &g = kp.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.isize || j >= g.jsize) return;
   bool fu, fv;
   const int si = ghost_source(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
   const int sj = ghost_source(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
-  const long long s = si + (long long)g.isize * sj, d = i + (long long)g.isize * j, n = g.plane;
+  const long long s = si + (long long)kp.wpitch * sj, d = i + (long long)g.isize * j;
 #pragma unroll
   for (int v = 0; v < 4; ++v) {
-    double x = (double)w[s + v * n] + (double)w[s + (4 + v) * n];
+    double x = (double)w[s + v * kp.wplane] + (double)w[s + (4 + v) * kp.wplane];
     if ((v == E2D_IU && fu) || (v == E2D_IV && fv)) x = -x;
-    u[d + v * n] = x;
+    u[d + v * g.plane] = x;
   }
 }
 
@@ -293,44 +335,60 @@ __global__ void __launch_bounds__(NT) k_f32c_dt(const KParams32 kp, const float 
                                                 DevClock *clk, const int slot) {
   const KGeom &g = kp.g;
   float best = -1.0f;
-  int bcell = -1;
+  long long bcell = -1;
   const long long ncell = (long long)g.nx * g.ny;
   for (long long k = blockIdx.x * (long long)NT + threadIdx.x; k < ncell; k += (long long)gridDim.x * NT) {
     const int j = (int)(k / g.nx), i = (int)(k - (long long)j * g.nx);
-    const int c = (i + 2) + g.isize * (j + 2);
-    const float t = cfl_term32(kp.ph, w[c], w[c + g.plane], w[c + 2 * g.plane], w[c + 3 * g.plane]);
+    const long long c = (i + 2) + (long long)kp.wpitch * (j + 2);
+    const float t = cfl_term32(kp.ph, w[c], w[c + kp.wplane], w[c + 2 * kp.wplane], w[c + 3 * kp.wplane]);
     if (t > best) best = t, bcell = c;
   }
-  block_cfl_fold(kp, best, bcell, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status);
+  warp_cfl_fold(kp, best, bcell, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status);
 }
 
 // ------------------------------------------------------------ the step
-template <int RS>
-__global__ void __launch_bounds__(NT, 4)
-    k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
-                DevClock *clk, const int use_clock, const double host_dt, double *__restrict__ dt_trace) {
-  extern __shared__ float sm[];
-  float *sQ = sm;                    // [4][QH][QW]
-  float *sXm = sQ + 4 * QH * QW;     // [4][TY][XW] XMIN states, then x-fluxes
-  float *sXp = sXm + 4 * TY * XW;    // [4][TY][XW] XMAX states
-  float *sYm = sXp + 4 * TY * XW;    // [4][YH][TX] YMIN states, then y-fluxes
-  float *sYp = sYm + 4 * YH * TX;    // [4][YH][TX] YMAX states
+// Loads the 4 conserved hi values of array row r for the lane's two columns
+// (c0, c0 + 1), ghosts mapped; `direct`: both columns are interior cells of
+// an aligned pair, read as one float2 per variable.
+__device__ __forceinline__ void load_row(const KParams32 &kp, const float *__restrict__ w, int r, int c0,
+                                         bool direct, float2 out[4]) {
+  const KGeom &g = kp.g;
+  bool fv;
+  const int rr = min(max(r, 0), g.jsize - 1);
+  const int sr = ghost_source(rr, g.ny, g.bc_ymin, g.bc_ymax, fv);
+  const float *row = w + (long long)sr * kp.wpitch;
+  if (direct) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = __ldg(reinterpret_cast<const float2 *>(row + v * kp.wplane + c0));
+  } else {
+    bool f0, f1;
+    const int s0 = ghost_source(min(max(c0, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f0);
+    const int s1 = ghost_source(min(max(c0 + 1, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f1);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = make_float2(__ldg(row + v * kp.wplane + s0), __ldg(row + v * kp.wplane + s1));
+    if (f0) out[E2D_IU].x = -out[E2D_IU].x;
+    if (f1) out[E2D_IU].y = -out[E2D_IU].y;
+  }
+  if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
+}
 
+template <int RS, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
+                DevClock *clk, const int use_clock, const double host_dt) {
   const KGeom &g = kp.g;
   const KPhys<float> &ph = kp.ph;
   const int tid = threadIdx.x;
-  const long long P = g.plane;
+  const int lane = tid & 31;
 
-  // dt of this step (FP64, src/main.cpp:128-134), computed by one thread: the
-  // FP64 pipe runs at 1/70 of the FP32 rate, so per-thread divisions here
-  // would dominate the kernel
+  // dt of this step (FP64, src/main.cpp:128-134) by one thread per block
   __shared__ double s_dt[3];
   __shared__ int s_run, s_slot;
   if (tid == 0) {
-    double dt = host_dt, t = 0.0;
+    double dt = host_dt;
     int run = 1, slot = 0;
     if (use_clock) {
-      t = clk->t;
+      const double t = clk->t;
       const double t_end = clk->t_end;
       run = t < t_end;
       slot = clk->nstep & 1;
@@ -346,161 +404,187 @@ __global__ void __launch_bounds__(NT, 4)
   }
   __syncthreads();
   if (!s_run) return;
-  const double dt = s_dt[0];
   const int slot = s_slot;
-  const float dtdx = (float)s_dt[1];
-  const float dtdy = (float)s_dt[2];
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const float2 dtdx = f2((float)s_dt[1]);
+  const float2 dtdy = f2((float)s_dt[2]);
 
-  // stage 1: primitives of the tile and its halo; ghosts via the boundary map
-  for (int k = tid; k < QH * QW; k += NT) {
-    const int y = k / QW, x = k - y * QW;
-    int gi = i0 + x, gj = j0 + y;
-    if (gi >= g.isize) gi = g.isize - 1;
-    if (gj >= g.jsize) gj = g.jsize - 1;
-    bool fu, fv;
-    const int si = ghost_source(gi, g.nx, g.bc_xmin, g.bc_xmax, fu);
-    const int sj = ghost_source(gj, g.ny, g.bc_ymin, g.bc_ymax, fv);
-    const long long s = si + (long long)g.isize * sj;
-    const float rho = w_in[s], e = w_in[s + P];
-    float mx = w_in[s + 2 * P], my = w_in[s + 3 * P];
-    if (fu) mx = -mx;
-    if (fv) my = -my;
-    float d, p, ux, uy;
-    prims32(ph, rho, e, mx, my, d, p, ux, uy);
-    sQ[k] = d;
-    sQ[QH * QW + k] = p;
-    sQ[2 * QH * QW + k] = ux;
-    sQ[3 * QH * QW + k] = uy;
-  }
-  __syncthreads();
-
-  // stage 2: slopes, sources and face states
-  const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
-  const float st = ph.slope_type;
-  for (int k = tid; k < YH * XW; k += NT) {
-    const int yy = k / XW, xx = k - yy * XW;
-    const bool xin = (xx >= 1) && (xx <= TX);
-    const bool yin = (yy >= 1) && (yy <= TY);
-    if (!xin && !yin) continue;
-    const int c = (yy + 1) * QW + (xx + 1);
-    float qc[4], dqx[4], dqy[4], s0[4];
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const float *Pq = sQ + v * QH * QW;
-      qc[v] = Pq[c];
-      dqx[v] = slope32(st_kind, st, qc[v], Pq[c + 1], Pq[c - 1]);
-      dqy[v] = slope32(st_kind, st, qc[v], Pq[c + QW], Pq[c - QW]);
-    }
-    sources32(ph, qc, dqx, dqy, s0);
-    if (yin) {
-      const int o = (yy - 1) * XW + xx;
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float h = 0.5f * dqx[v], sx = 0.5f * s0[v] * dtdx;
-        float fm = qc[v] - h + sx, fp = qc[v] + h + sx;
-        if (v == E2D_ID) fm = fmaxf(fm, ph.smallr), fp = fmaxf(fp, ph.smallr);
-        if (xx >= 1) sXm[v * TY * XW + o] = fm;
-        if (xx <= TX) sXp[v * TY * XW + o] = fp;
-      }
-    }
-    if (xin) {
-      const int o = yy * TX + (xx - 1);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float h = 0.5f * dqy[v], sy = 0.5f * s0[v] * dtdy;
-        float fm = qc[v] - h + sy, fp = qc[v] + h + sy;
-        if (v == E2D_ID) fm = fmaxf(fm, ph.smallr), fp = fmaxf(fp, ph.smallr);
-        if (yy >= 1) sYm[v * YH * TX + o] = fm;
-        if (yy <= TY) sYp[v * YH * TX + o] = fp;
-      }
-    }
-  }
-  __syncthreads();
-
-  // stage 3: Riemann solves; scaled fluxes replace the right-hand states
-  constexpr int NXF = (TX + 1) * TY;
-  constexpr int NYF = TX * (TY + 1);
-  for (int k = tid; k < NXF + NYF; k += NT) {
-    float ql[4], qr[4], f[4];
-    if (k < NXF) {
-      const int y = k / (TX + 1), fx = k - y * (TX + 1);
-      const int ol = y * XW + fx, orr = ol + 1;
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        ql[v] = sXp[v * TY * XW + ol];
-        qr[v] = sXm[v * TY * XW + orr];
-      }
-      riemann32<RS>(ph, ql, qr, f);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) sXm[v * TY * XW + orr] = f[v] * dtdx;
-    } else {
-      const int kk = k - NXF;
-      const int fy = kk / TX, x = kk - fy * TX;
-      const int ol = fy * TX + x, orr = ol + TX;
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
-        ql[vs] = sYp[v * YH * TX + ol];
-        qr[vs] = sYm[v * YH * TX + orr];
-      }
-      riemann32<RS>(ph, ql, qr, f);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
-        sYm[v * YH * TX + orr] = f[vs] * dtdy;
-      }
-    }
-  }
-  __syncthreads();
-
-  // stage 4: compensated update and the next step's CFL term
+  const int nsx = (g.nx + OUTW - 1) / OUTW;
+  const int SH = kp.strip_h;
+  const int nsy = (g.ny + SH - 1) / SH;
+  const int strip = blockIdx.x * WPB + (tid >> 5);
   float best = -1.0f;
-  int bcell = -1;
-  for (int k = tid; k < TX * TY; k += NT) {
-    const int y = k / TX, x = k - y * TX;
-    const int gi = i0 + 2 + x, gj = j0 + 2 + y;
-    if (gi < g.nx + 2 && gj < g.ny + 2) {
-      const long long s = gi + (long long)g.isize * gj;
-      float nh[4];
+  long long bcell = -1;
+  if (strip < nsx * nsy) {
+    const int sx = strip % nsx, sy = strip / nsx;
+    const int cb = 2 + sx * OUTW;       // array column of the strip's first output column
+    const int rb = 2 + sy * SH;         // array row of the strip's first output row
+    const int re = min(rb + SH, g.ny + 2);
+    const int c0 = cb - 2 + 2 * lane;   // the lane's columns: c0, c0 + 1
+    const bool direct = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1);
+    const bool writer = (lane >= 1) && (lane <= 30) && (c0 < g.nx + 2);
+    const C2 k = make_c2(ph);
+    const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
+    const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
+
+    float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
+    float2 ymax_prev[4];  // YMAX states of row m-1
+    float2 fx_prev[4];    // x-fluxes of row m-1: .x face (c0|c1), .y face (c1|c1+1)
+    float2 fy_prev[4];    // y-flux of the face between rows m-2 and m-1
+#pragma unroll
+    for (int v = 0; v < 4; ++v) ymax_prev[v] = fx_prev[v] = fy_prev[v] = f2(0.0f);
+    float2 pf[4];  // conserved hi of row m+1, loaded one iteration ahead
+    {
+      float2 u[4];
+      load_row(kp, w_in, rb - 2, c0, direct, u);
+      prims2(k, u[0], u[1], u[2], u[3], qa);
+      load_row(kp, w_in, rb - 1, c0, direct, u);
+      prims2(k, u[0], u[1], u[2], u[3], qb);
+      load_row(kp, w_in, rb, c0, direct, pf);
+    }
+    // march: row n = m + 1 is loaded; faces of row m built; y-flux of face
+    // (m-1|m); update of row m-1
+    for (int m = rb - 1; m <= re; ++m) {
+      float2 qc[4];
+      {
+        float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
+        // issue the next row's loads before this row's arithmetic
+        if (m + 2 <= re + 1) load_row(kp, w_in, m + 2, c0, direct, pf);
+        prims2(k, u[0], u[1], u[2], u[3], qc);
+      }
+      // the update of row m-1 reads its (hi, lo): issue those loads early too
+      const bool upd = (m >= rb + 1) && writer;
+      const long long ubase = c0 + (long long)kp.wpitch * (m - 1);
+      float2 uhi[4], ulo[4];
+      if (upd) {
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          uhi[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + v * kp.wplane));
+          ulo[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + (4 + v) * kp.wplane));
+        }
+      }
+      // slopes of row m (x from the neighbour lanes, y from rows m-1, m+1)
+      float2 dqx[4], dqy[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        const float du = (sXm[v * TY * XW + y * XW + x + 1] - sXm[v * TY * XW + y * XW + x + 2]) +
-                         (sYm[v * YH * TX + (y + 1) * TX + x] - sYm[v * YH * TX + (y + 2) * TX + x]);
-        const float hi = w_in[s + v * P];
-        float lo = w_in[s + (4 + v) * P];
-        // TwoSum(hi, du)
-        const float sum = hi + du;
-        const float bb = sum - hi;
-        const float err = (hi - (sum - bb)) + (du - bb);
-        lo = lo + err;
-        // Fast2Sum(sum, lo), |sum| >= |lo|
-        const float h2 = sum + lo;
-        const float l2 = lo - (h2 - sum);
-        w_out[s + v * P] = h2;
-        w_out[s + (4 + v) * P] = l2;
-        nh[v] = h2;
+        const float left = __shfl_up_sync(0xffffffffu, qb[v].y, 1);
+        const float right = __shfl_down_sync(0xffffffffu, qb[v].x, 1);
+        if (st_kind == 0) {
+          dqx[v] = f2(0.0f);
+          dqy[v] = f2(0.0f);
+        } else {
+          dqx[v] = slope2(k, qb[v], make_float2(qb[v].y, right), make_float2(left, qb[v].x));
+          dqy[v] = slope2(k, qb[v], qc[v], qa[v]);
+        }
       }
-      if (use_clock) {
-        const float tt = cfl_term32(ph, nh[E2D_ID], nh[E2D_IP], nh[E2D_IU], nh[E2D_IV]);
-        if (tt > best) best = tt, bcell = (int)s;
+      // trace sources (src/HydroBaseFunctor.h:246-249)
+      float2 s0[4];
+      {
+        const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
+        const float2 div = dqx[E2D_IU] + dqy[E2D_IV];
+        const float2 ir = rcp2(r);
+        s0[E2D_ID] = neg2(fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r)));
+        s0[E2D_IP] = neg2(fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p)));
+        s0[E2D_IU] = neg2(fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir)));
+        s0[E2D_IV] = neg2(fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir)));
+      }
+      // x faces of row m and their fluxes (needed for rows rb..re-1)
+      float2 fx[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
+      if (m >= rb && m < re) {
+        float2 xl[4], xr[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const float2 h = k.half * dqx[v];
+          const float2 s = k.half * s0[v] * dtdx;
+          float2 xmin = (qb[v] - h) + s;
+          float2 xmax = (qb[v] + h) + s;
+          if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
+          xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
+          xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
+        }
+        riemann2<RS>(ph, k, xl, xr, fx);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
+      }
+      // y faces of row m; flux of face (m-1|m) from the saved YMAX of row m-1
+      float2 ymin[4], ymax[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const float2 h = k.half * dqy[v];
+        const float2 s = k.half * s0[v] * dtdy;
+        ymin[v] = (qb[v] - h) + s;
+        ymax[v] = (qb[v] + h) + s;
+      }
+      ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
+      ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
+      float2 fy[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
+      if (m >= rb) {
+        // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
+        float2 yl[4] = {ymax_prev[E2D_ID], ymax_prev[E2D_IP], ymax_prev[E2D_IV], ymax_prev[E2D_IU]};
+        float2 yr[4] = {ymin[E2D_ID], ymin[E2D_IP], ymin[E2D_IV], ymin[E2D_IU]};
+        float2 f[4];
+        riemann2<RS>(ph, k, yl, yr, f);
+        fy[E2D_ID] = f[E2D_ID] * dtdy;
+        fy[E2D_IP] = f[E2D_IP] * dtdy;
+        fy[E2D_IU] = f[E2D_IV] * dtdy;
+        fy[E2D_IV] = f[E2D_IU] * dtdy;
+      }
+      // compensated update of row m-1
+      if (m >= rb + 1) {
+        float2 fxl[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) fxl[v] = make_float2(__shfl_up_sync(0xffffffffu, fx_prev[v].y, 1), fx_prev[v].x);
+        if (upd) {
+          const long long base = ubase;
+          float2 nh[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            // +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
+            const float2 du = (fxl[v] - fx_prev[v]) + (fy_prev[v] - fy[v]);
+            const float2 hi = uhi[v];
+            float2 lo = ulo[v];
+            const float2 sum = hi + du;           // TwoSum(hi, du)
+            const float2 bb = sum - hi;
+            const float2 err = (hi - (sum - bb)) + (du - bb);
+            lo = lo + err;
+            const float2 h2 = sum + lo;           // Fast2Sum(sum, lo)
+            const float2 l2 = lo - (h2 - sum);
+            *reinterpret_cast<float2 *>(w_out + base + v * kp.wplane) = h2;
+            *reinterpret_cast<float2 *>(w_out + base + (4 + v) * kp.wplane) = l2;
+            nh[v] = h2;
+          }
+          if (use_clock) {
+            const float2 t = cfl_term2(k, idx, nh);
+            if (t.x > best) best = t.x, bcell = base;
+            if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, bcell = base + 1;
+          }
+        }
+      }
+      // roll
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        qa[v] = qb[v];
+        qb[v] = qc[v];
+        ymax_prev[v] = ymax[v];
+        fx_prev[v] = fx[v];
+        fy_prev[v] = fy[v];
       }
     }
   }
   if (!use_clock) return;
-  __syncthreads();  // this block's writes of w_out are visible to thread 0
-  block_cfl_fold(kp, best, bcell, w_out, &clk->acc[slot ^ 1], &clk->status);
+  warp_cfl_fold(kp, best, bcell, w_out, &clk->acc[slot ^ 1], &clk->status);
 
   // the last block to finish advances the loop state (src/main.cpp:139-143)
+  __syncthreads();
   if (tid == 0) {
     __threadfence();
-    const unsigned int nblocks = gridDim.x * gridDim.y;
+    const unsigned int nblocks = gridDim.x;
     const unsigned int ticket = atomicAdd(&clk->done_blocks, 1u);
     if (ticket == nblocks - 1) {
       __threadfence();
+      const double dt = s_dt[0];
       const int ns = clk->nstep;
       const int tslot = ns - clk->trace_base;
-      if (dt_trace && tslot >= 0 && tslot < clk->trace_cap) dt_trace[tslot] = dt;
+      if (clk->trace && tslot >= 0 && tslot < clk->trace_cap) clk->trace[tslot] = dt;
       if (!(dt > 0.0) || nonfinite64(dt)) clk->status |= E2D_FLAG_BAD_DT;
       clk->dt = dt;
       clk->t = clk->t + dt;  // only this block writes t during the step
@@ -514,6 +598,16 @@ __global__ void __launch_bounds__(NT, 4)
 
 }  // namespace
 
+// Rows per warp strip: the largest of 64, 32, 16 that still gives every SM
+// at least 16 strips (one strip per warp at full residency); taller strips
+// cost less halo ((h + 4) / h rows loaded per output row).
+int default_strip_h(int nx, int ny) {
+  const long long nsx = (nx + OUTW - 1) / OUTW;
+  for (int h = 64; h > 16; h /= 2)
+    if (nsx * ((ny + h - 1) / h) >= 152LL * 16) return h;
+  return 16;
+}
+
 void make_kparams32(const e2d_params &p, KParams32 *kp) {
   KParams64 k64;
   make_kparams(p, &k64);
@@ -523,28 +617,25 @@ void make_kparams32(const e2d_params &p, KParams32 *kp) {
   kp->ph = KPhys<float>{(float)d.gamma0, (float)d.gamma6, (float)d.cfl, (float)d.slope_type,
                         (float)d.smallr, (float)d.smallc, (float)d.smallp, (float)d.smallpp,
                         (float)d.gm1, (float)d.entho, (float)d.smallc2, (float)d.dx, (float)d.dy};
+  kp->wpitch = (p.isize + 3) & ~3;
+  kp->wplane = (long long)kp->wpitch * p.jsize;
+  kp->variant = 1;
+  kp->strip_h = default_strip_h(p.nx, p.ny);
 }
 
-cudaError_t configure_f32c_kernels() {
-  const int smem = (int)(kSmemFloats * sizeof(float));
-  cudaError_t e = cudaFuncSetAttribute(k_step_f32c<E2D_RIEMANN_HLLC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_step_f32c<E2D_RIEMANN_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_step_f32c<E2D_RIEMANN_APPROX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-}
+cudaError_t configure_f32c_kernels() { return cudaSuccess; }
 
 cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w, cudaStream_t s) {
-  const long long n = kp.g.plane;
-  const int blocks = (int)((n + 255) / 256 < 65535 * 8 ? (n + 255) / 256 : 65535 * 8);
-  k_f32c_from_f64<<<blocks, 256, 0, s>>>(kp.g, u, w);
+  dim3 block(64, 4);
+  dim3 grid((kp.g.isize + 63) / 64, (kp.g.jsize + 3) / 4);
+  k_f32c_from_f64<<<grid, block, 0, s>>>(kp, u, w);
   return cudaGetLastError();
 }
 
 cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, cudaStream_t s) {
   dim3 block(64, 4);
   dim3 grid((kp.g.isize + 63) / 64, (kp.g.jsize + 3) / 4);
-  k_f32c_to_f64<<<grid, block, 0, s>>>(kp.g, w, u);
+  k_f32c_to_f64<<<grid, block, 0, s>>>(kp, w, u);
   return cudaGetLastError();
 }
 
@@ -556,22 +647,33 @@ cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, i
   return cudaGetLastError();
 }
 
-cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
-                             DevClock *clk, int use_clock, double host_dt, double *dt_trace,
-                             cudaStream_t s) {
-  dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
-  const size_t smem = kSmemFloats * sizeof(float);
+template <int MINB>
+static void launch_step_minb(const KParams32 &kp, int riemann, int blocks, const float *w_in, float *w_out,
+                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_step_f32c<E2D_RIEMANN_HLLC><<<grid, NT, smem, s>>>(kp, w_in, w_out, clk, use_clock, host_dt, dt_trace);
+      k_step_f32c<E2D_RIEMANN_HLLC, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     case E2D_RIEMANN_HLL:
-      k_step_f32c<E2D_RIEMANN_HLL><<<grid, NT, smem, s>>>(kp, w_in, w_out, clk, use_clock, host_dt, dt_trace);
+      k_step_f32c<E2D_RIEMANN_HLL, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     default:
-      k_step_f32c<E2D_RIEMANN_APPROX><<<grid, NT, smem, s>>>(kp, w_in, w_out, clk, use_clock, host_dt, dt_trace);
+      k_step_f32c<E2D_RIEMANN_APPROX, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
   }
+}
+
+cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
+                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
+  const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
+  const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
+  const int blocks = (nsx * nsy + WPB - 1) / WPB;
+  // register budget variant: 0 -> as many registers as the code wants
+  // (3 blocks per SM), 1 -> 128 registers (4 blocks per SM, small spill)
+  if (kp.variant == 0)
+    launch_step_minb<1>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s);
+  else
+    launch_step_minb<4>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s);
   return cudaGetLastError();
 }
 

@@ -56,11 +56,18 @@ struct KParams64 {
 };
 
 // FP32 step with FP64 copies of the constants the exact dt recompute uses.
+// FP32C state arrays use a row pitch `wpitch` (isize rounded up to a
+// multiple of 4 floats) so every row starts on a 16-byte boundary.
 struct KParams32 {
   KGeom g;
   KPhys<float> ph;
   KPhys<double> ph64;
+  int wpitch;
+  long long wplane;  // wpitch * jsize
+  int variant;       // step kernel register-budget variant (see launch_f32c_step)
+  int strip_h;       // rows per warp strip of the step kernel
 };
+int default_strip_h(int nx, int ny);
 
 // Device-resident loop state of the time loop of src/main.cpp:100-145.
 struct DevClock {
@@ -77,6 +84,7 @@ struct DevClock {
   // FP32 path: the step of parity n reads the CFL maximum of its input from
   // acc[n & 1] and folds that of its output into acc[(n + 1) & 1]
   unsigned long long acc[2];
+  double *trace;  // FP32 path: device dt trace (trace_cap entries) or null
 };
 
 enum : unsigned int {
@@ -122,8 +130,7 @@ cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, c
 // CFL maximum of a state (interior) into clk->acc[slot] (slot < 0: invdt_bits).
 cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s);
 cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
-                             DevClock *clk, int use_clock, double host_dt, double *dt_trace,
-                             cudaStream_t s);
+                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s);
 
 // FP64 reductions over the interior (e2d_reduce.cu): per-variable sums and
 // the L1 difference of two states, deterministic (fixed summation tree).
