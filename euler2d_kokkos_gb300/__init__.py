@@ -115,6 +115,21 @@ SIGNATURES = {
     "e2d_eval_device": ([_P, _I, _I, _V, _V, _D, _D], _I),
     "e2d_conservation": ([_V, _I, _V], _I),
     "e2d_l1_diff": ([_V, _I, _V, _I, _I, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
+    "e2d_batch_create": ([_I, ctypes.c_size_t, _I, ctypes.POINTER(_V)], _I),
+    "e2d_batch_destroy": ([_V], _I),
+    "e2d_batch_last_error": ([_V], ctypes.c_char_p),
+    "e2d_batch_instance_bytes": ([_P], ctypes.c_size_t),
+    "e2d_batch_free_bytes": ([_V, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)], _I),
+    "e2d_batch_admit": ([_V, _P, _D, _V, ctypes.POINTER(_I)], _I),
+    "e2d_batch_run": ([_V, _I, ctypes.POINTER(_I)], _I),
+    "e2d_batch_query": ([_V, _I, ctypes.POINTER(_D), ctypes.POINTER(_I), ctypes.POINTER(_I)], _I),
+    "e2d_batch_get_state": ([_V, _I, _V, _I], _I),
+    "e2d_batch_release": ([_V, _I], _I),
+    "e2d_batch_stats": ([_V, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I)], _I),
+    "e2d_batch_stream": ([_V, ctypes.POINTER(_V)], _I),
+    "e2d_batch_set_tuning": ([_V, _I, _V], _I),
+    "e2d_batch_get_tuning": ([_V, ctypes.POINTER(_I), _V], _I),
+    "e2d_batch_autotune": ([_V, _I], _I),
     "e2d_set_profiling": ([_V, _I], _I),
     "e2d_kernel_times": ([_V, _I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(_D),
                           ctypes.POINTER(ctypes.c_long), ctypes.POINTER(_I)], _I),
@@ -348,6 +363,105 @@ class HydroRun:
 
     def reset_kernel_times(self):
         self._lib.e2d_reset_kernel_times(self._h)
+
+
+class Batch:
+    """Many independent FP32-compensated solves of uneven size in one device
+    pool, advanced together (e2d_batch_* in include/e2d.h)."""
+
+    def __init__(self, riemann: str = "hllc", pool_bytes: int = 8 << 30, max_instances: int = 1024):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.e2d_batch_create(RIEMANN[riemann], int(pool_bytes), int(max_instances),
+                                          ctypes.byref(h)), "e2d_batch_create")
+        self._h = h
+        self.riemann = riemann
+        self.shapes = {}
+
+    def _ck(self, status, where):
+        if status != 0:
+            detail = (self._lib.e2d_batch_last_error(self._h) or b"").decode()
+            raise E2DError(status, where, detail)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.e2d_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def instance_bytes(params: HydroParams) -> int:
+        return int(load_library().e2d_batch_instance_bytes(ctypes.byref(params._raw)))
+
+    def free_bytes(self):
+        f, l = ctypes.c_size_t(), ctypes.c_size_t()
+        self._ck(self._lib.e2d_batch_free_bytes(self._h, ctypes.byref(f), ctypes.byref(l)), "free_bytes")
+        return f.value, l.value
+
+    def admit(self, params: HydroParams, t_end: float, u0: np.ndarray | None = None) -> int:
+        i = ctypes.c_int()
+        ptr = None
+        if u0 is not None:
+            u0 = np.ascontiguousarray(u0, dtype=np.float64)
+            ptr = u0.ctypes.data
+        self._ck(self._lib.e2d_batch_admit(self._h, ctypes.byref(params._raw), float(t_end), ptr,
+                                           ctypes.byref(i)), "admit")
+        self.shapes[i.value] = (4, params.ny + 4, params.nx + 4)
+        return i.value
+
+    def run(self, iterations: int) -> int:
+        n = ctypes.c_int()
+        self._ck(self._lib.e2d_batch_run(self._h, int(iterations), ctypes.byref(n)), "run")
+        return n.value
+
+    def query(self, id: int):
+        t, ns, a = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        self._ck(self._lib.e2d_batch_query(self._h, int(id), ctypes.byref(t), ctypes.byref(ns),
+                                           ctypes.byref(a)), "query")
+        return t.value, ns.value, bool(a.value)
+
+    def get_state(self, id: int) -> np.ndarray:
+        out = np.empty(self.shapes[id], dtype=np.float64)
+        self._ck(self._lib.e2d_batch_get_state(self._h, int(id), out.ctypes.data, LAYOUT_LEFT), "get_state")
+        return out
+
+    def release(self, id: int):
+        self._ck(self._lib.e2d_batch_release(self._h, int(id)), "release")
+        self.shapes.pop(id, None)
+
+    def stats(self):
+        c, n = ctypes.c_longlong(), ctypes.c_int()
+        self._ck(self._lib.e2d_batch_stats(self._h, ctypes.byref(c), ctypes.byref(n)), "stats")
+        return c.value, n.value
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        self._ck(self._lib.e2d_batch_stream(self._h, ctypes.byref(s)), "stream")
+        return s.value or 0
+
+    def set_tuning(self, variant: int = -1, strip_h=None):
+        arr = None if strip_h is None else (ctypes.c_int * 3)(*strip_h)
+        self._ck(self._lib.e2d_batch_set_tuning(self._h, int(variant), arr), "set_tuning")
+
+    def get_tuning(self):
+        v = ctypes.c_int()
+        arr = (ctypes.c_int * 3)()
+        self._ck(self._lib.e2d_batch_get_tuning(self._h, ctypes.byref(v), arr), "get_tuning")
+        return v.value, list(arr)
+
+    def autotune(self, iters_per_trial: int = 2):
+        self._ck(self._lib.e2d_batch_autotune(self._h, int(iters_per_trial)), "autotune")
 
 
 EVAL = {"primitives": (0, 4, 5), "slopes": (1, 20, 8), "trace_xmin": (2, 12, 4), "trace_xmax": (3, 12, 4),

@@ -253,7 +253,9 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
   make_kparams(p, &s->kp);
   make_kparams32(p, &s->kp32);
   if (const char *v = std::getenv("E2D_F32C_VARIANT")) s->kp32.variant = std::atoi(v);
-  if (const char *v = std::getenv("E2D_F32C_STRIP_H")) s->kp32.strip_h = std::atoi(v) > 0 ? std::atoi(v) : s->kp32.strip_h;
+  // strip heights are whole 16-row CFL fold units
+  if (const char *v = std::getenv("E2D_F32C_STRIP_H"))
+    if (std::atoi(v) > 0) s->kp32.strip_h = (std::atoi(v) + 15) / 16 * 16;
   auto fail = [&](int status) {
     e2d_destroy(s);
     return status;

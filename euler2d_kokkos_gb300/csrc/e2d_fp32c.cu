@@ -30,6 +30,7 @@ namespace {
 constexpr int LANES = 32;
 constexpr int OUTW = 60;   // output columns per warp strip (lanes 1..30)
 constexpr int WPB = 4;     // warps (strips) per block
+constexpr int CFL_UNIT_ROWS = 16;  // rows of a CFL fold unit (strip heights are multiples)
 constexpr int NT = WPB * LANES;
 
 // ------------------------------------------------------------ packed FP32
@@ -257,16 +258,6 @@ __device__ __forceinline__ float2 cfl_term2(const C2 &k, float2 idx, const float
   return fma2(c + abs2(q[E2D_IU]), f2(idx.x), (c + abs2(q[E2D_IV])) * f2(idx.y));
 }
 
-__device__ __forceinline__ float cfl_term32(const KPhys<float> &ph, float rho, float e, float mx, float my) {
-  const float d = fmaxf(rho, ph.smallr);
-  const float inv = 1.0f / d;
-  const float ux = mx * inv, uy = my * inv;
-  const float ei = e * inv - 0.5f * (ux * ux + uy * uy);
-  const float p = fmaxf(ph.gm1 * d * ei, d * ph.smallp);
-  const float c = sqrtf(ph.gamma0 * p * inv);
-  return (c + fabsf(ux)) / ph.dx + (c + fabsf(uy)) / ph.dy;
-}
-
 // Warp arg-max of an FP32 term, then lane 0 folds the winner's FP64 term
 // into *target -- skipped when the FP32 term is more than 1e-4 below the
 // running maximum (FP32 terms are within ~1e-6 of the FP64 ones, so such a
@@ -330,20 +321,39 @@ __global__ void k_f32c_to_f64(const KParams32 kp, const float *__restrict__ w, d
   }
 }
 
-// CFL maximum of a compensated state.
+// CFL maximum of a compensated state, folded per fold unit exactly as the
+// step kernels fold it (same candidate cells, same order), so a dt computed
+// here equals the one the previous step folded.
 __global__ void __launch_bounds__(NT) k_f32c_dt(const KParams32 kp, const float *__restrict__ w,
-                                                DevClock *clk, const int slot) {
+                                                unsigned long long *target, unsigned int *status) {
   const KGeom &g = kp.g;
-  float best = -1.0f;
-  long long bcell = -1;
-  const long long ncell = (long long)g.nx * g.ny;
-  for (long long k = blockIdx.x * (long long)NT + threadIdx.x; k < ncell; k += (long long)gridDim.x * NT) {
-    const int j = (int)(k / g.nx), i = (int)(k - (long long)j * g.nx);
-    const long long c = (i + 2) + (long long)kp.wpitch * (j + 2);
-    const float t = cfl_term32(kp.ph, w[c], w[c + kp.wplane], w[c + 2 * kp.wplane], w[c + 3 * kp.wplane]);
-    if (t > best) best = t, bcell = c;
+  const int lane = threadIdx.x & 31;
+  const int nsx = (g.nx + OUTW - 1) / OUTW;
+  const int nsy = (g.ny + CFL_UNIT_ROWS - 1) / CFL_UNIT_ROWS;
+  const C2 k = make_c2(kp.ph);
+  const float2 idx = make_float2(1.0f / kp.ph.dx, 1.0f / kp.ph.dy);
+  for (int u = blockIdx.x * WPB + (threadIdx.x >> 5); u < nsx * nsy; u += gridDim.x * WPB) {
+    const int sx = u % nsx, sy = u / nsx;
+    const int cb = 2 + sx * OUTW;
+    const int rb = 2 + sy * CFL_UNIT_ROWS;
+    const int re = min(rb + CFL_UNIT_ROWS, g.ny + 2);
+    const int c0 = cb - 2 + 2 * lane;
+    const bool writer = (lane >= 1) && (lane <= 30) && (c0 < g.nx + 2);
+    float best = -1.0f;
+    long long bcell = -1;
+    if (writer) {
+      for (int r = rb; r < re; ++r) {
+        const long long base = c0 + (long long)kp.wpitch * r;
+        float2 h[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) h[v] = __ldg(reinterpret_cast<const float2 *>(w + base + v * kp.wplane));
+        const float2 t = cfl_term2(k, idx, h);
+        if (t.x > best) best = t.x, bcell = base;
+        if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, bcell = base + 1;
+      }
+    }
+    warp_cfl_fold(kp, best, bcell, w, target, status);
   }
-  warp_cfl_fold(kp, best, bcell, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status);
 }
 
 // ------------------------------------------------------------ the step
@@ -372,12 +382,189 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
   if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
 }
 
+// One warp marches strip (sx, sy) of an instance: rows rb-2 .. re+1 are
+// read, rows rb .. re-1 written.  With a target, the CFL term of the new
+// state is folded into *target once per fold unit -- the strip's 60 output
+// columns by 16 rows of the interior -- so that the set of FP64-recomputed
+// candidates depends only on the grid, never on the strip height, the
+// kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS).
+template <int RS>
+__device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
+                                            float *__restrict__ w_out, const float2 dtdx,
+                                            const float2 dtdy, const int sx, const int sy,
+                                            const int lane, unsigned long long *target,
+                                            unsigned int *status) {
+  float best = -1.0f;
+  long long bcell = -1;
+  const KGeom &g = kp.g;
+  const KPhys<float> &ph = kp.ph;
+  const int SH = kp.strip_h;
+  const int cb = 2 + sx * OUTW;       // array column of the strip's first output column
+  const int rb = 2 + sy * SH;         // array row of the strip's first output row
+  const int re = min(rb + SH, g.ny + 2);
+  const int c0 = cb - 2 + 2 * lane;   // the lane's columns: c0, c0 + 1
+  const bool direct = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1);
+  const bool writer = (lane >= 1) && (lane <= 30) && (c0 < g.nx + 2);
+  const C2 k = make_c2(ph);
+  const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
+  const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
+
+  float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
+  float2 ymax_prev[4];  // YMAX states of row m-1
+  float2 fx_prev[4];    // x-fluxes of row m-1: .x face (c0|c1), .y face (c1|c1+1)
+  float2 fy_prev[4];    // y-flux of the face between rows m-2 and m-1
+#pragma unroll
+  for (int v = 0; v < 4; ++v) ymax_prev[v] = fx_prev[v] = fy_prev[v] = f2(0.0f);
+  float2 pf[4];  // conserved hi of row m+1, loaded one iteration ahead
+  {
+    float2 u[4];
+    load_row(kp, w_in, rb - 2, c0, direct, u);
+    prims2(k, u[0], u[1], u[2], u[3], qa);
+    load_row(kp, w_in, rb - 1, c0, direct, u);
+    prims2(k, u[0], u[1], u[2], u[3], qb);
+    load_row(kp, w_in, rb, c0, direct, pf);
+  }
+  // march: row n = m + 1 is loaded; faces of row m built; y-flux of face
+  // (m-1|m); update of row m-1
+  for (int m = rb - 1; m <= re; ++m) {
+    float2 qc[4];
+    {
+      float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
+      // issue the next row's loads before this row's arithmetic
+      if (m + 2 <= re + 1) load_row(kp, w_in, m + 2, c0, direct, pf);
+      prims2(k, u[0], u[1], u[2], u[3], qc);
+    }
+    // the update of row m-1 reads its (hi, lo): issue those loads early too
+    const bool upd = (m >= rb + 1) && writer;
+    const long long ubase = c0 + (long long)kp.wpitch * (m - 1);
+    float2 uhi[4], ulo[4];
+    if (upd) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        uhi[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + v * kp.wplane));
+        ulo[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + (4 + v) * kp.wplane));
+      }
+    }
+    // slopes of row m (x from the neighbour lanes, y from rows m-1, m+1)
+    float2 dqx[4], dqy[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const float left = __shfl_up_sync(0xffffffffu, qb[v].y, 1);
+      const float right = __shfl_down_sync(0xffffffffu, qb[v].x, 1);
+      if (st_kind == 0) {
+        dqx[v] = f2(0.0f);
+        dqy[v] = f2(0.0f);
+      } else {
+        dqx[v] = slope2(k, qb[v], make_float2(qb[v].y, right), make_float2(left, qb[v].x));
+        dqy[v] = slope2(k, qb[v], qc[v], qa[v]);
+      }
+    }
+    // trace sources (src/HydroBaseFunctor.h:246-249)
+    float2 s0[4];
+    {
+      const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
+      const float2 div = dqx[E2D_IU] + dqy[E2D_IV];
+      const float2 ir = rcp2(r);
+      s0[E2D_ID] = neg2(fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r)));
+      s0[E2D_IP] = neg2(fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p)));
+      s0[E2D_IU] = neg2(fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir)));
+      s0[E2D_IV] = neg2(fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir)));
+    }
+    // x faces of row m and their fluxes (needed for rows rb..re-1)
+    float2 fx[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
+    if (m >= rb && m < re) {
+      float2 xl[4], xr[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const float2 h = k.half * dqx[v];
+        const float2 s = k.half * s0[v] * dtdx;
+        float2 xmin = (qb[v] - h) + s;
+        float2 xmax = (qb[v] + h) + s;
+        if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
+        xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
+        xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
+      }
+      riemann2<RS>(ph, k, xl, xr, fx);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
+    }
+    // y faces of row m; flux of face (m-1|m) from the saved YMAX of row m-1
+    float2 ymin[4], ymax[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const float2 h = k.half * dqy[v];
+      const float2 s = k.half * s0[v] * dtdy;
+      ymin[v] = (qb[v] - h) + s;
+      ymax[v] = (qb[v] + h) + s;
+    }
+    ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
+    ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
+    float2 fy[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
+    if (m >= rb) {
+      // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
+      float2 yl[4] = {ymax_prev[E2D_ID], ymax_prev[E2D_IP], ymax_prev[E2D_IV], ymax_prev[E2D_IU]};
+      float2 yr[4] = {ymin[E2D_ID], ymin[E2D_IP], ymin[E2D_IV], ymin[E2D_IU]};
+      float2 f[4];
+      riemann2<RS>(ph, k, yl, yr, f);
+      fy[E2D_ID] = f[E2D_ID] * dtdy;
+      fy[E2D_IP] = f[E2D_IP] * dtdy;
+      fy[E2D_IU] = f[E2D_IV] * dtdy;
+      fy[E2D_IV] = f[E2D_IU] * dtdy;
+    }
+    // compensated update of row m-1
+    if (m >= rb + 1) {
+      float2 fxl[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fxl[v] = make_float2(__shfl_up_sync(0xffffffffu, fx_prev[v].y, 1), fx_prev[v].x);
+      if (upd) {
+        const long long base = ubase;
+        float2 nh[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          // +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
+          const float2 du = (fxl[v] - fx_prev[v]) + (fy_prev[v] - fy[v]);
+          const float2 hi = uhi[v];
+          float2 lo = ulo[v];
+          const float2 sum = hi + du;           // TwoSum(hi, du)
+          const float2 bb = sum - hi;
+          const float2 err = (hi - (sum - bb)) + (du - bb);
+          lo = lo + err;
+          const float2 h2 = sum + lo;           // Fast2Sum(sum, lo)
+          const float2 l2 = lo - (h2 - sum);
+          *reinterpret_cast<float2 *>(w_out + base + v * kp.wplane) = h2;
+          *reinterpret_cast<float2 *>(w_out + base + (4 + v) * kp.wplane) = l2;
+          nh[v] = h2;
+        }
+        if (target) {
+          const float2 t = cfl_term2(k, idx, nh);
+          if (t.x > best) best = t.x, bcell = base;
+          if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, bcell = base + 1;
+        }
+      }
+      const int r = m - 1;
+      if (target && (((r - 2) % CFL_UNIT_ROWS) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
+        warp_cfl_fold(kp, best, bcell, w_out, target, status);
+        best = -1.0f;
+        bcell = -1;
+      }
+    }
+    // roll
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qa[v] = qb[v];
+      qb[v] = qc[v];
+      ymax_prev[v] = ymax[v];
+      fx_prev[v] = fx[v];
+      fy_prev[v] = fy[v];
+    }
+  }
+}
+
 template <int RS, int MINB>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
                 DevClock *clk, const int use_clock, const double host_dt) {
   const KGeom &g = kp.g;
-  const KPhys<float> &ph = kp.ph;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
 
@@ -412,166 +599,10 @@ __global__ void __launch_bounds__(NT, MINB)
   const int SH = kp.strip_h;
   const int nsy = (g.ny + SH - 1) / SH;
   const int strip = blockIdx.x * WPB + (tid >> 5);
-  float best = -1.0f;
-  long long bcell = -1;
-  if (strip < nsx * nsy) {
-    const int sx = strip % nsx, sy = strip / nsx;
-    const int cb = 2 + sx * OUTW;       // array column of the strip's first output column
-    const int rb = 2 + sy * SH;         // array row of the strip's first output row
-    const int re = min(rb + SH, g.ny + 2);
-    const int c0 = cb - 2 + 2 * lane;   // the lane's columns: c0, c0 + 1
-    const bool direct = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1);
-    const bool writer = (lane >= 1) && (lane <= 30) && (c0 < g.nx + 2);
-    const C2 k = make_c2(ph);
-    const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
-    const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
-
-    float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
-    float2 ymax_prev[4];  // YMAX states of row m-1
-    float2 fx_prev[4];    // x-fluxes of row m-1: .x face (c0|c1), .y face (c1|c1+1)
-    float2 fy_prev[4];    // y-flux of the face between rows m-2 and m-1
-#pragma unroll
-    for (int v = 0; v < 4; ++v) ymax_prev[v] = fx_prev[v] = fy_prev[v] = f2(0.0f);
-    float2 pf[4];  // conserved hi of row m+1, loaded one iteration ahead
-    {
-      float2 u[4];
-      load_row(kp, w_in, rb - 2, c0, direct, u);
-      prims2(k, u[0], u[1], u[2], u[3], qa);
-      load_row(kp, w_in, rb - 1, c0, direct, u);
-      prims2(k, u[0], u[1], u[2], u[3], qb);
-      load_row(kp, w_in, rb, c0, direct, pf);
-    }
-    // march: row n = m + 1 is loaded; faces of row m built; y-flux of face
-    // (m-1|m); update of row m-1
-    for (int m = rb - 1; m <= re; ++m) {
-      float2 qc[4];
-      {
-        float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
-        // issue the next row's loads before this row's arithmetic
-        if (m + 2 <= re + 1) load_row(kp, w_in, m + 2, c0, direct, pf);
-        prims2(k, u[0], u[1], u[2], u[3], qc);
-      }
-      // the update of row m-1 reads its (hi, lo): issue those loads early too
-      const bool upd = (m >= rb + 1) && writer;
-      const long long ubase = c0 + (long long)kp.wpitch * (m - 1);
-      float2 uhi[4], ulo[4];
-      if (upd) {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          uhi[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + v * kp.wplane));
-          ulo[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + (4 + v) * kp.wplane));
-        }
-      }
-      // slopes of row m (x from the neighbour lanes, y from rows m-1, m+1)
-      float2 dqx[4], dqy[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float left = __shfl_up_sync(0xffffffffu, qb[v].y, 1);
-        const float right = __shfl_down_sync(0xffffffffu, qb[v].x, 1);
-        if (st_kind == 0) {
-          dqx[v] = f2(0.0f);
-          dqy[v] = f2(0.0f);
-        } else {
-          dqx[v] = slope2(k, qb[v], make_float2(qb[v].y, right), make_float2(left, qb[v].x));
-          dqy[v] = slope2(k, qb[v], qc[v], qa[v]);
-        }
-      }
-      // trace sources (src/HydroBaseFunctor.h:246-249)
-      float2 s0[4];
-      {
-        const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
-        const float2 div = dqx[E2D_IU] + dqy[E2D_IV];
-        const float2 ir = rcp2(r);
-        s0[E2D_ID] = neg2(fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r)));
-        s0[E2D_IP] = neg2(fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p)));
-        s0[E2D_IU] = neg2(fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir)));
-        s0[E2D_IV] = neg2(fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir)));
-      }
-      // x faces of row m and their fluxes (needed for rows rb..re-1)
-      float2 fx[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
-      if (m >= rb && m < re) {
-        float2 xl[4], xr[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const float2 h = k.half * dqx[v];
-          const float2 s = k.half * s0[v] * dtdx;
-          float2 xmin = (qb[v] - h) + s;
-          float2 xmax = (qb[v] + h) + s;
-          if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
-          xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
-          xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
-        }
-        riemann2<RS>(ph, k, xl, xr, fx);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
-      }
-      // y faces of row m; flux of face (m-1|m) from the saved YMAX of row m-1
-      float2 ymin[4], ymax[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float2 h = k.half * dqy[v];
-        const float2 s = k.half * s0[v] * dtdy;
-        ymin[v] = (qb[v] - h) + s;
-        ymax[v] = (qb[v] + h) + s;
-      }
-      ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
-      ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
-      float2 fy[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
-      if (m >= rb) {
-        // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
-        float2 yl[4] = {ymax_prev[E2D_ID], ymax_prev[E2D_IP], ymax_prev[E2D_IV], ymax_prev[E2D_IU]};
-        float2 yr[4] = {ymin[E2D_ID], ymin[E2D_IP], ymin[E2D_IV], ymin[E2D_IU]};
-        float2 f[4];
-        riemann2<RS>(ph, k, yl, yr, f);
-        fy[E2D_ID] = f[E2D_ID] * dtdy;
-        fy[E2D_IP] = f[E2D_IP] * dtdy;
-        fy[E2D_IU] = f[E2D_IV] * dtdy;
-        fy[E2D_IV] = f[E2D_IU] * dtdy;
-      }
-      // compensated update of row m-1
-      if (m >= rb + 1) {
-        float2 fxl[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) fxl[v] = make_float2(__shfl_up_sync(0xffffffffu, fx_prev[v].y, 1), fx_prev[v].x);
-        if (upd) {
-          const long long base = ubase;
-          float2 nh[4];
-#pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            // +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
-            const float2 du = (fxl[v] - fx_prev[v]) + (fy_prev[v] - fy[v]);
-            const float2 hi = uhi[v];
-            float2 lo = ulo[v];
-            const float2 sum = hi + du;           // TwoSum(hi, du)
-            const float2 bb = sum - hi;
-            const float2 err = (hi - (sum - bb)) + (du - bb);
-            lo = lo + err;
-            const float2 h2 = sum + lo;           // Fast2Sum(sum, lo)
-            const float2 l2 = lo - (h2 - sum);
-            *reinterpret_cast<float2 *>(w_out + base + v * kp.wplane) = h2;
-            *reinterpret_cast<float2 *>(w_out + base + (4 + v) * kp.wplane) = l2;
-            nh[v] = h2;
-          }
-          if (use_clock) {
-            const float2 t = cfl_term2(k, idx, nh);
-            if (t.x > best) best = t.x, bcell = base;
-            if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, bcell = base + 1;
-          }
-        }
-      }
-      // roll
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        qa[v] = qb[v];
-        qb[v] = qc[v];
-        ymax_prev[v] = ymax[v];
-        fx_prev[v] = fx[v];
-        fy_prev[v] = fy[v];
-      }
-    }
-  }
+  if (strip < nsx * nsy)
+    march_strip<RS>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
+                    use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status);
   if (!use_clock) return;
-  warp_cfl_fold(kp, best, bcell, w_out, &clk->acc[slot ^ 1], &clk->status);
 
   // the last block to finish advances the loop state (src/main.cpp:139-143)
   __syncthreads();
@@ -596,7 +627,139 @@ __global__ void __launch_bounds__(NT, MINB)
   }
 }
 
+// ------------------------------------------------------------ batches
+// The loop-state advance of src/main.cpp:139-143 plus the next dt (:128-134)
+// for one instance; run by the instance's last strip of an iteration.
+__device__ __forceinline__ void batch_finalize(BatchInst &I) {
+  const int n = I.nstep;
+  const double dt = I.dt;
+  if (!(dt > 0.0) || nonfinite64(dt)) I.status |= E2D_FLAG_BAD_DT;
+  const double t = I.t + dt;
+  I.t = t;
+  I.nstep = n + 1;
+  I.par ^= 1;
+  I.acc[n & 1] = 0ull;
+  const double inv_dt = __longlong_as_double((long long)I.acc[(n + 1) & 1]);
+  double dtn = I.kp.ph64.cfl / inv_dt;
+  if (t + dtn > I.t_end) dtn = I.t_end - t;
+  I.dt = dtn;
+  I.dtdx = (float)(dtn / I.kp.ph64.dx);
+  I.dtdy = (float)(dtn / I.kp.ph64.dy);
+  I.active = (t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
+  I.done = 0u;
+}
+
+// One iteration of a batch: every warp takes strips of the global strip list
+// (instances concatenated) with a grid-sized stride, marches them with its
+// instance's own dt, folds the instance's next CFL maximum, and the last
+// strip of each instance advances that instance's loop state.  Results of an
+// instance do not depend on the other instances in the batch.
+template <int RS, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_batch_f32c(BatchInst *__restrict__ insts, const int *__restrict__ list_slots,
+                 const int *__restrict__ strip_begin, const int n_inst, const int total_strips) {
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * WPB;
+  for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < total_strips; w += nwarps) {
+    // instance k with strip_begin[k] <= w < strip_begin[k + 1]
+    int lo = 0, hi = n_inst;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (strip_begin[mid] <= w)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    BatchInst &I = insts[list_slots[lo]];
+    if (!I.active) continue;  // warp-uniform
+    const KParams32 &kp = I.kp;
+    const int par = I.par;
+    const int strip = w - strip_begin[lo];
+    march_strip<RS>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx, strip / I.nsx,
+                    lane, &I.acc[(I.nstep + 1) & 1], &I.status);
+    if (lane == 0) {
+      __threadfence();
+      const unsigned int ticket = atomicAdd(&I.done, 1u);
+      if (ticket == (unsigned)I.nstrips - 1u) {
+        __threadfence();
+        batch_finalize(I);
+        __threadfence();
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_batch_arm(BatchInst *I) {
+  const double inv_dt = __longlong_as_double((long long)I->acc[I->nstep & 1]);
+  double dt = I->kp.ph64.cfl / inv_dt;
+  if (I->t + dt > I->t_end) dt = I->t_end - I->t;
+  I->dt = dt;
+  I->dtdx = (float)(dt / I->kp.ph64.dx);
+  I->dtdy = (float)(dt / I->kp.ph64.dy);
+  I->active = (I->t < I->t_end) && !(I->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
+  I->done = 0u;
+}
+
 }  // namespace
+
+int strips_of(const KParams32 &kp) {
+  const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
+  return nsx * ((kp.g.ny + kp.strip_h - 1) / kp.strip_h);
+}
+
+template <int MINB>
+static void launch_batch_minb(int riemann, BatchInst *insts, const int *slots, const int *sb, int n,
+                              int total, int grid, cudaStream_t s) {
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC:
+      k_batch_f32c<E2D_RIEMANN_HLLC, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      break;
+    case E2D_RIEMANN_HLL:
+      k_batch_f32c<E2D_RIEMANN_HLL, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      break;
+    default:
+      k_batch_f32c<E2D_RIEMANN_APPROX, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      break;
+  }
+}
+
+cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const int *list_slots,
+                              const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
+                              cudaStream_t s) {
+  if (n_inst <= 0 || total_strips <= 0) return cudaSuccess;
+  if (variant == 0)
+    launch_batch_minb<1>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s);
+  else
+    launch_batch_minb<4>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_arm(BatchInst *inst, cudaStream_t s) {
+  k_batch_arm<<<1, 1, 0, s>>>(inst);
+  return cudaGetLastError();
+}
+
+int batch_blocks_per_sm(int riemann, int variant) {
+  int n = 0;
+  cudaError_t e;
+  const bool v0 = variant == 0;
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC:
+      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLLC, 1>, NT, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLLC, 4>, NT, 0);
+      break;
+    case E2D_RIEMANN_HLL:
+      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLL, 1>, NT, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLL, 4>, NT, 0);
+      break;
+    default:
+      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_APPROX, 1>, NT, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_APPROX, 4>, NT, 0);
+      break;
+  }
+  return (e == cudaSuccess && n > 0) ? n : 1;
+}
 
 // Rows per warp strip: the largest of 64, 32, 16 that still gives every SM
 // at least 16 strips (one strip per warp at full residency); taller strips
@@ -639,12 +802,17 @@ cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s) {
-  const long long ncell = (long long)kp.g.nx * kp.g.ny;
-  long long blocks = (ncell + NT - 1) / NT;
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  k_f32c_dt<<<(int)blocks, NT, 0, s>>>(kp, w, clk, slot);
+cudaError_t launch_f32c_dt_to(const KParams32 &kp, const float *w, unsigned long long *target,
+                              unsigned int *status, cudaStream_t s) {
+  const long long units = (long long)((kp.g.nx + OUTW - 1) / OUTW) * ((kp.g.ny + CFL_UNIT_ROWS - 1) / CFL_UNIT_ROWS);
+  long long blocks = (units + WPB - 1) / WPB;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_f32c_dt<<<(int)blocks, NT, 0, s>>>(kp, w, target, status);
   return cudaGetLastError();
+}
+
+cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s) {
+  return launch_f32c_dt_to(kp, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status, s);
 }
 
 template <int MINB>

@@ -129,8 +129,40 @@ cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w,
 cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, cudaStream_t s);
 // CFL maximum of a state (interior) into clk->acc[slot] (slot < 0: invdt_bits).
 cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s);
+cudaError_t launch_f32c_dt_to(const KParams32 &kp, const float *w, unsigned long long *target,
+                              unsigned int *status, cudaStream_t s);
 cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
                              DevClock *clk, int use_clock, double host_dt, cudaStream_t s);
+
+// ---------------------------------------------------------------- batches
+// One instance of a batch (device table entry): its grid, its two
+// compensated states and its own time loop.  The loop state is advanced by
+// the last strip of the instance to finish each iteration.
+struct BatchInst {
+  KParams32 kp;
+  float *w[2];
+  double t, t_end, dt;          // dt: of the pending step
+  unsigned long long acc[2];    // CFL maxima by step parity
+  int par;                      // w[par] holds the current state
+  int active;                   // 1 while t < t_end
+  int nstep;
+  int nsx, nstrips;             // strips of the step kernel
+  float dtdx, dtdy;             // of the pending step
+  unsigned int done;            // strips finished in the current iteration
+  unsigned int status;          // E2D_FLAG_* bits
+};
+
+// One iteration over every strip of every listed instance: list entry k is
+// table slot list_slots[k]; strip_begin[k] is its first global strip
+// (n_inst + 1 entries, the last = total_strips).
+cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const int *list_slots,
+                              const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
+                              cudaStream_t s);
+// dt, dt/dx, dt/dy and `active` of an instance from acc[nstep & 1].
+cudaError_t launch_batch_arm(BatchInst *inst, cudaStream_t s);
+// Resident blocks per SM of the batch kernel variant (occupancy).
+int batch_blocks_per_sm(int riemann, int variant);
+int strips_of(const KParams32 &kp);
 
 // FP64 reductions over the interior (e2d_reduce.cu): per-variable sums and
 // the L1 difference of two states, deterministic (fixed summation tree).

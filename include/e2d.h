@@ -200,6 +200,47 @@ int e2d_godunov_unsplit_noalloc(const e2d_params *p, double *u_in, double *u_out
  * replayed from cached CUDA graphs.  Blocks until done. */
 int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double *dt_trace);
 
+/* ---------------------------------------------------------------------------
+ * Batched solves.  No counterpart in the reference, which runs one grid per
+ * process: this build's serving mode keeps many independent simulations of
+ * uneven size resident in one device memory pool and advances all active
+ * ones together, one kernel launch per iteration (each instance with its own
+ * dt and t_end), replayed from CUDA graphs.  Arithmetic: FP32 compensated.
+ * One Riemann solver per batch.  A handle is used from one host thread.
+ * ------------------------------------------------------------------------- */
+typedef struct e2d_batch e2d_batch;
+/* A batch with a device pool of pool_bytes and room for max_instances. */
+int e2d_batch_create(int riemann, size_t pool_bytes, int max_instances, e2d_batch **out);
+int e2d_batch_destroy(e2d_batch *b);
+const char *e2d_batch_last_error(const e2d_batch *b);
+/* Pool bytes an instance with these parameters needs to be admitted. */
+size_t e2d_batch_instance_bytes(const e2d_params *p);
+int e2d_batch_free_bytes(const e2d_batch *b, size_t *free_bytes, size_t *largest_block);
+/* Admit one solve: its initial condition is u0 (host, LayoutLeft FP64, whole
+ * array) or, if u0 is NULL, params->problemType's; it runs until t_end.
+ * E2D_ENOMEM when the pool or the instance table has no room. */
+int e2d_batch_admit(e2d_batch *b, const e2d_params *p, double t_end, const double *u0, int *id);
+/* Advance every active instance by up to `iterations` steps; *n_active
+ * receives the number of instances still short of their t_end. */
+int e2d_batch_run(e2d_batch *b, int iterations, int *n_active);
+/* Loop state of an instance as of the last run (t, steps, still active). */
+int e2d_batch_query(e2d_batch *b, int id, double *t, int *nstep, int *active);
+/* Current state of an instance (hi + lo in FP64, ghosts filled), host copy. */
+int e2d_batch_get_state(e2d_batch *b, int id, double *host, int layout);
+/* Free an instance's pool bytes and slot. */
+int e2d_batch_release(e2d_batch *b, int id);
+/* Interior cell-updates done by run calls so far; instances in the pool. */
+int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_instances);
+/* The batch's CUDA stream (a cudaStream_t). */
+int e2d_batch_stream(e2d_batch *b, void **stream);
+/* Tuning: register-budget variant of the batch kernel (0 or 1) and rows per
+ * strip for the size classes max(nx, ny) <= 192, <= 512, > 512.  Results do
+ * not depend on them.  e2d_batch_autotune times the candidates on the live
+ * batch (its iterations advance the instances) and keeps the fastest. */
+int e2d_batch_set_tuning(e2d_batch *b, int variant, const int strip_h[3]);
+int e2d_batch_get_tuning(const e2d_batch *b, int *variant, int strip_h[3]);
+int e2d_batch_autotune(e2d_batch *b, int iters_per_trial);
+
 /* Building blocks of the FP64 step evaluated on the device, n independent
  * inputs each (host arrays; the per-function known-answer interface of the
  * reference's HydroBaseFunctor, src/HydroBaseFunctor.h):

@@ -1,0 +1,130 @@
+"""Batched solves: each result is the same alone and in the mix (bit for
+bit), equals the single-simulation FP32C path, respects its own t_end, and
+admission follows the pool's free bytes."""
+import numpy as np
+import pytest
+
+import euler2d_kokkos_gb300 as e2d
+from euler2d_kokkos_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+POOL = 2 << 30
+
+
+def run_to_end(batch, max_iters=100000, chunk=16):
+    n = 1
+    it = 0
+    while n > 0 and it < max_iters:
+        n = batch.run(chunk)
+        it += chunk
+    return it
+
+
+def small_mix(n=10, seed=7):
+    return W.mixed_batch(n, seed=seed, max_side=192)
+
+
+def test_batch_mix_equals_alone(gpu_lib):
+    solves = small_mix()
+    with e2d.Batch(pool_bytes=POOL) as b:
+        ids = [b.admit(s.params, s.t_end, s.u0) for s in solves]
+        run_to_end(b)
+        mixed = [b.get_state(i) for i in ids]
+        ends = [b.query(i) for i in ids]
+    for s, got, (t, ns, active) in zip(solves, mixed, ends):
+        assert not active and t == s.t_end
+        with e2d.Batch(pool_bytes=POOL) as alone:
+            i = alone.admit(s.params, s.t_end, s.u0)
+            run_to_end(alone)
+            assert np.array_equal(alone.get_state(i), got)
+            assert alone.query(i)[1] == ns
+
+
+def test_batch_equals_single_simulation_path(gpu_lib):
+    s = small_mix(2, seed=3)[1]
+    with e2d.Batch(pool_bytes=POOL) as b:
+        i = b.admit(s.params, s.t_end, s.u0)
+        run_to_end(b)
+        got = b.get_state(i)
+        t_b, n_b, _ = b.query(i)
+    with e2d.HydroRun(s.params, init_problem=False) as h:
+        h.set_state(0, s.u0)
+        h.set_state(1, s.u0)
+        t, ns = 0.0, 0
+        while t < s.t_end:
+            t, ns, tr = h.step_n(64, s.t_end, t, ns)
+            if len(tr) == 0:
+                break
+        single = h.current(ns)
+    assert (t, ns) == (t_b, n_b)
+    assert np.array_equal(got, single)
+
+
+def test_batch_tuning_does_not_change_results(gpu_lib):
+    solves = small_mix(6, seed=11)
+    outs = []
+    for tuning in [(1, [16, 32, 64]), (0, [64, 16, 32]), (1, [8, 8, 8])]:
+        with e2d.Batch(pool_bytes=POOL) as b:
+            b.set_tuning(*tuning)
+            ids = [b.admit(s.params, s.t_end, s.u0) for s in solves]
+            run_to_end(b)
+            outs.append([b.get_state(i) for i in ids])
+    for other in outs[1:]:
+        for a, c in zip(outs[0], other):
+            assert np.array_equal(a, c)
+
+
+def test_batch_autotune_keeps_results(gpu_lib):
+    solves = small_mix(6, seed=12)
+    with e2d.Batch(pool_bytes=POOL) as b:
+        ids = [b.admit(s.params, s.t_end, s.u0) for s in solves]
+        b.autotune(2)
+        run_to_end(b)
+        tuned = [b.get_state(i) for i in ids]
+    with e2d.Batch(pool_bytes=POOL) as b:
+        ids = [b.admit(s.params, s.t_end, s.u0) for s in solves]
+        run_to_end(b)
+        plain = [b.get_state(i) for i in ids]
+    for a, c in zip(tuned, plain):
+        assert np.array_equal(a, c)
+
+
+def test_batch_admission_by_free_bytes(gpu_lib):
+    s = small_mix(1, seed=5)[0]
+    need = e2d.Batch.instance_bytes(s.params)
+    with e2d.Batch(pool_bytes=3 * need) as b:
+        a = b.admit(s.params, s.t_end, s.u0)
+        c = b.admit(s.params, s.t_end, s.u0)
+        free, _ = b.free_bytes()
+        with pytest.raises(e2d.E2DError) as ei:
+            for _ in range(4):
+                b.admit(s.params, s.t_end, s.u0)
+        assert ei.value.status == 2  # E2D_ENOMEM
+        b.release(a)
+        d = b.admit(s.params, s.t_end, s.u0)  # room again
+        run_to_end(b)
+        assert np.array_equal(b.get_state(c), b.get_state(d))
+
+
+def test_batch_fp32c_accuracy_vs_fp64(gpu_lib):
+    """A batched FP32C solve against the FP64 path (bit-identical to the
+    reference) at the same final time: relative L1 of density <= 1e-5."""
+    s = small_mix(2, seed=9)[0]
+    with e2d.Batch(pool_bytes=POOL) as b:
+        i = b.admit(s.params, s.t_end, s.u0)
+        run_to_end(b)
+        got = b.get_state(i)
+    p64 = s.params.copy()
+    p64.precision = e2d.PRECISION_FP64
+    with e2d.HydroRun(p64.init(), init_problem=False) as h:
+        h.set_state(0, s.u0)
+        h.set_state(1, s.u0)
+        t, ns = 0.0, 0
+        while t < s.t_end:
+            t, ns, tr = h.step_n(256, s.t_end, t, ns)
+            if len(tr) == 0:
+                break
+        ref = h.current(ns)
+    rho, rref = got[0, 2:-2, 2:-2], ref[0, 2:-2, 2:-2]
+    assert np.abs(rho - rref).sum() / np.abs(rref).sum() < 1e-5
