@@ -56,6 +56,13 @@ def parse():
                     help="steps of the CPU baseline sample (0: sized to ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
+                    help="step: one grid (default); batch: 512 mixed solves batched vs one at a "
+                         "time; serve: Poisson arrivals into the batched loop")
+    ap.add_argument("--instances", type=int, default=512)
+    ap.add_argument("--sample", type=int, default=24, help="solves timed one at a time (batch mode)")
+    ap.add_argument("--rates", default="", help="arrival rates (solves/s) for serve mode, comma-separated")
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
     a = ap.parse_args()
     if a.problem is None:
         a.problem = "blast" if a.precision == "fp64" else "four_quadrant"
@@ -352,11 +359,119 @@ def l1_check(e2d, nx, t_end):
     return res
 
 
+def fp64_l1_of(e2d, solve, got):
+    """Relative L1 density error of a batched FP32C result against the FP64
+    path (bit-identical to the reference) run to the same t_end."""
+    p64 = solve.params.copy()
+    p64.precision = e2d.PRECISION_FP64
+    with e2d.HydroRun(p64.init(), init_problem=False) as h:
+        h.set_state(0, solve.u0)
+        t, ns = 0.0, 0
+        while t < solve.t_end:
+            prev = ns
+            t, ns, _ = h.step_n(512, solve.t_end, t, ns, want_trace=False)
+            if ns == prev:
+                break
+        ref = h.current(ns)
+    a, r = got[0, 2:-2, 2:-2], ref[0, 2:-2, 2:-2]
+    return float(np.abs(a - r).sum() / np.abs(r).sum())
+
+
+BATCH_WORKLOAD = ("mixed solves: blasts (pressure ratio 10..1e4) and four-quadrant problems, sides "
+                  "log-uniform 64..1024 (multiples of 16), t_end U[0.05,0.25], HLLC, CFL 0.8, seed 0")
+SERVE_WORKLOAD = ("Poisson arrivals of blasts, four-quadrant problems and shocked bubbles (Mach 1.2..3, "
+                  "density ratio 0.1..10), grids 64^2..2048^2, t_end U[0.05,0.25], 150 GB pool, HLLC, CFL 0.8")
+
+
+def batch_summary(instances, sample):
+    """Mixed 64^2-1024^2 blasts and four-quadrant problems (seed 0), each to
+    its own t_end: one batched run of all of them against the same kind of
+    solves run one at a time, FP32 compensated, HLLC, CFL 0.8."""
+    import euler2d_kokkos_gb300 as e2d
+    from euler2d_kokkos_gb300 import serving, workloads
+
+    solves = workloads.mixed_batch(instances, seed=0)
+    stride = max(1, len(solves) // sample)
+    sample_idx = list(range(0, len(solves), stride))[:sample]
+    # accuracy: the smallest sampled solves against the FP64 path
+    small = sorted(sample_idx, key=lambda k: solves[k].cells)[:3]
+    bstats, states = serving.run_batched(solves, pool_bytes=64 << 30, keep=set(small))
+    seq = serving.run_one_at_a_time([solves[k] for k in sample_idx])
+    l1 = [fp64_l1_of(e2d, solves[k], states[k]) for k in small if k in states]
+    return {"workload": f"{len(solves)} {BATCH_WORKLOAD}", "instances": len(solves),
+            "cells_total": sum(s.cells for s in solves),
+            "tuning": {"variant": bstats.tuning[0], "strip_h_per_class": bstats.tuning[1]},
+            "value": bstats.gcell_per_s, "unit": METRIC,
+            "batched": {"value": bstats.gcell_per_s, "seconds": bstats.seconds,
+                        "cell_updates": bstats.cell_updates, "launch_iterations": bstats.iterations},
+            "one_at_a_time": {"value": seq.gcell_per_s, "seconds": seq.seconds, "solves": seq.solves,
+                              "cell_updates": seq.cell_updates,
+                              "sample": f"{len(sample_idx)} of the {len(solves)} solves, every {stride}th"},
+            "batched_over_one_at_a_time": bstats.gcell_per_s / seq.gcell_per_s if seq.gcell_per_s else None,
+            "rel_l1_density_vs_fp64": l1}
+
+
+def serve_summary(rates, seconds, max_requests):
+    """Open-loop Poisson arrivals of mixed solves (the batch mix plus shocked
+    bubbles, grids 64^2..2048^2) into a 150 GB pool; one entry per arrival
+    rate with latency percentiles and aggregate throughput."""
+    from euler2d_kokkos_gb300 import serving, workloads
+
+    results = []
+    for rate in rates:
+        n = max(8, int(rate * seconds))
+        solves = workloads.mixed_batch(min(n, max_requests), seed=1, max_side=2048, bubbles=True)
+        st = serving.serve(solves, rate, pool_bytes=150 << 30, time_limit_s=seconds * 4)
+        results.append({"rate_per_s": rate, "requests": len(solves), "completed": st.solves,
+                        "value": st.gcell_per_s, "seconds": st.seconds, **st.percentiles()})
+    return results
+
+
+def mode_line(value, mode, config_, extra):
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": 1, "steps": 0, "warmup": 0,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (compensated hi/lo state, FP64 dt)", "data": "synthetic", "impl": "gb300",
+            "mode": mode, "config": config_}
+    line.update(extra)
+    return line
+
+
+def batch_mode(args):
+    with ClockSampler(0) as clocks:
+        b = batch_summary(args.instances, args.sample)
+    line = mode_line(b["value"], "batch", {"workload": b["workload"], "instances": b["instances"],
+                                           "cells_total": b["cells_total"], "tuning": b["tuning"]},
+                     {k: b[k] for k in ("batched", "one_at_a_time", "batched_over_one_at_a_time",
+                                        "rel_l1_density_vs_fp64")})
+    line["steps"] = b["batched"]["launch_iterations"]
+    line["ms_per_step"] = b["batched"]["seconds"] * 1e3 / max(line["steps"], 1)
+    line["clocks"] = clocks.summary()
+    print(json.dumps(line), flush=True)
+
+
+def serve_mode(args):
+    rates = [float(r) for r in args.rates.split(",") if r] or [4.0, 8.0, 16.0, 24.0, 32.0]
+    with ClockSampler(0) as clocks:
+        sweep = serve_summary(rates, args.serve_seconds, args.instances)
+    best = max(sweep, key=lambda r: r["value"])
+    line = mode_line(best["value"], "serve", {"workload": SERVE_WORKLOAD}, {"sweep": sweep})
+    line["clocks"] = clocks.summary()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference_arm(args, rank)
+        return
+    if args.mode == "batch":
+        if rank == 0:
+            batch_mode(args)
+        return
+    if args.mode == "serve":
+        if rank == 0:
+            serve_mode(args)
         return
 
     import torch
@@ -410,6 +525,9 @@ def main():
             "ms_per_step": s["ms"] / args.steps,
             "roofline": roofline(s["kernels"], "fp32c", sc, "k_step_f32c"),
             "accuracy": l1_check(e2d, 1024, 0.3)}
+        # batched mixed solves against one at a time, and one loaded serving point
+        line["batch"] = batch_summary(512, 24)
+        line["serve"] = {"workload": SERVE_WORKLOAD, "sweep": serve_summary([32.0], 10.0, 320)}
 
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.problem, min(nx, 4096), args.cpu_sample_steps)

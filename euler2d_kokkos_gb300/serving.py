@@ -29,6 +29,7 @@ class RunStats:
     solves: int = 0
     iterations: int = 0
     latencies: list = field(default_factory=list)
+    tuning: tuple = ()
 
     @property
     def gcell_per_s(self) -> float:
@@ -103,8 +104,9 @@ def run_one_at_a_time(solves, chunk=256):
             h.set_state(0, s.u0)
             t, ns = 0.0, 0
             while t < s.t_end:
-                t, ns, tr = h.step_n(chunk, s.t_end, t, ns, want_trace=False)
-                if ns == 0:
+                prev = ns
+                t, ns, _ = h.step_n(chunk, s.t_end, t, ns, want_trace=False)
+                if ns == prev:
                     break
             h.current(ns)
             stats.cell_updates += ns * s.params.nx * s.params.ny

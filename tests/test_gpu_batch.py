@@ -128,3 +128,25 @@ def test_batch_fp32c_accuracy_vs_fp64(gpu_lib):
         ref = h.current(ns)
     rho, rref = got[0, 2:-2, 2:-2], ref[0, 2:-2, 2:-2]
     assert np.abs(rho - rref).sum() / np.abs(rref).sum() < 1e-5
+
+
+def test_run_batched_and_serve_complete_every_solve(gpu_lib):
+    """The batched driver and the Poisson serving loop finish every request;
+    a kept final state equals the same solve run alone."""
+    from euler2d_kokkos_gb300 import serving
+
+    solves = small_mix(8, seed=21)
+    st, states = serving.run_batched(solves, pool_bytes=POOL, keep={0, 5})
+    assert st.solves == len(solves) and st.cell_updates > 0
+    for k in (0, 5):
+        with e2d.Batch(pool_bytes=POOL) as alone:
+            i = alone.admit(solves[k].params, solves[k].t_end, solves[k].u0)
+            run_to_end(alone)
+            assert np.array_equal(alone.get_state(i), states[k])
+    sv = serving.serve(solves, rate_per_s=500.0, pool_bytes=POOL)
+    assert sv.solves == len(solves) and len(sv.latencies) == len(solves)
+    assert sv.cell_updates == st.cell_updates
+    pct = sv.percentiles()
+    assert 0 < pct["p50_s"] <= pct["p95_s"] <= pct["p99_s"] <= pct["max_s"]
+    seq = serving.run_one_at_a_time(solves[:2])
+    assert seq.solves == 2 and seq.cell_updates > 0
