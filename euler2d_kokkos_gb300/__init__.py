@@ -115,6 +115,8 @@ SIGNATURES = {
     "e2d_eval_device": ([_P, _I, _I, _V, _V, _D, _D], _I),
     "e2d_conservation": ([_V, _I, _V], _I),
     "e2d_l1_diff": ([_V, _I, _V, _I, _I, ctypes.POINTER(_D), ctypes.POINTER(_D)], _I),
+    "e2d_radial_profile": ([_V, _I, _I, _V, _V, _V], _I),
+    "e2d_save_npy": ([ctypes.c_char_p, _V, ctypes.c_longlong], _I),
     "e2d_batch_create": ([_I, ctypes.c_size_t, _I, ctypes.POINTER(_V)], _I),
     "e2d_batch_destroy": ([_V], _I),
     "e2d_batch_last_error": ([_V], ctypes.c_char_p),
@@ -349,6 +351,17 @@ class HydroRun:
                                      ctypes.byref(a), ctypes.byref(b)), "l1_diff", self._h)
         return a.value, b.value
 
+    # -- Sedov post-processing (src/ComputeRadialProfileFunctor.h:83-165)
+    def radial_profile(self, which: int = 0, nbins: int = 0):
+        """(distances, mean density, cell count) in nbins rings about the box
+        centre over every cell of state `which` (nbins <= 0: [blast] nbins)."""
+        n = int(nbins) if nbins > 0 else int(self.params.blast_nbins)
+        d, prof = np.zeros(n), np.zeros(n)
+        cnt = np.zeros(n, dtype=np.int64)
+        _check(self._lib.e2d_radial_profile(self._h, int(which), n, d.ctypes.data, prof.ctypes.data,
+                                            cnt.ctypes.data), "radial_profile", self._h)
+        return d, prof, cnt
+
     # -- profiling
     def set_profiling(self, on: bool):
         _check(self._lib.e2d_set_profiling(self._h, int(bool(on))), "set_profiling")
@@ -467,6 +480,13 @@ class Batch:
 EVAL = {"primitives": (0, 4, 5), "slopes": (1, 20, 8), "trace_xmin": (2, 12, 4), "trace_xmax": (3, 12, 4),
         "trace_ymin": (4, 12, 4), "trace_ymax": (5, 12, 4), "riemann_approx": (6, 8, 4),
         "riemann_hll": (7, 8, 4), "riemann_hllc": (8, 8, 4)}
+
+
+def save_npy(path: str, data) -> None:
+    """A 1-D double array as an NPY 1.0 file, byte for byte as the
+    reference's cnpy::npy_save writes it (src/cnpy/cnpy.h:130-187)."""
+    a = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+    _check(load_library().e2d_save_npy(os.fsencode(path), a.ctypes.data, a.size), "save_npy")
 
 
 def eval_device(params: HydroParams, what: str, inputs: np.ndarray, dtdx: float = 0.0,

@@ -2,8 +2,9 @@
 (and the euler2d_gb300 command-line driver beside it).
 
 Translation units compile in parallel, one -gencode for sm_103a.  The FP64
-kernels are built with --fmad=false so that no multiply-add is contracted:
-their results are bit-identical to the reference's FP64 arithmetic.
+kernels are built with --fmad=false and host code with -ffp-contract=off so
+that no multiply-add is contracted: their results are bit-identical to the
+reference's FP64 arithmetic.
 """
 from __future__ import annotations
 
@@ -21,7 +22,9 @@ LIB = os.path.join(OUT, "libe2d_gb300.so")
 CLI = os.path.join(OUT, "euler2d_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+# host code: no FMA contraction either (aarch64 hosts would otherwise fuse
+# a*b + c in the parameter and ring-geometry arithmetic)
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 # (source, extra nvcc flags)

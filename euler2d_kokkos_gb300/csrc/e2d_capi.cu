@@ -3,6 +3,7 @@
 // both arithmetic modes (FP64 bit-identical, FP32 compensated).
 #include "e2d_internal.h"
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -565,6 +566,78 @@ int e2d_l1_diff(e2d_sim *a, int wa, e2d_sim *b, int wb, int var, double *l1_diff
   *l1_diff = r[0];
   *l1_ref = r[1];
   return E2D_OK;
+}
+
+int e2d_radial_profile(e2d_sim *s, int which, int nbins, double *distances, double *profile,
+                       long long *counts) {
+  if (!s || !distances || !profile || (which != 0 && which != 1))
+    return set_err(s, E2D_EINVAL, "bad radial_profile args");
+  const e2d_params &p = s->p;
+  if (nbins <= 0) nbins = p.blast_nbins;
+  if (nbins <= 0 || nbins > (1 << 24)) return set_err(s, E2D_EINVAL, "radial_profile: nbins out of range");
+  // src/ComputeRadialProfileFunctor.h:90-103
+  ProfileGeom g;
+  g.xmin = p.xmin;
+  g.ymin = p.ymin;
+  g.dx = p.dx;
+  g.dy = p.dy;
+  g.cx = (p.xmin + p.xmax) / 2;
+  g.cy = (p.ymin + p.ymax) / 2;
+  const double Dx = (p.xmax - p.xmin) / 2;
+  const double Dy = (p.ymax - p.ymin) / 2;
+  g.rmax = std::sqrt(Dx * Dx + Dy * Dy);
+  g.isize = p.isize;
+  g.jsize = p.jsize;
+  g.ghost = p.ghostWidth;
+  g.nbins = nbins;
+  double *u = nullptr;
+  int rc = fp64_view(s, which, &u);
+  if (rc != E2D_OK) return rc;
+  const size_t words = 1 + 4 * (size_t)nbins;
+  unsigned long long *scratch = nullptr;
+  unsigned int *flags = nullptr;
+  E2D_CK(s, cudaMallocAsync((void **)&scratch, sizeof(unsigned long long) * words + 16, s->stream), "profile alloc");
+  flags = reinterpret_cast<unsigned int *>(scratch + words);
+  std::vector<unsigned long long> host(words);
+  unsigned int hflags = 0;
+  cudaError_t e = launch_radial_profile(g, u, scratch, flags, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(host.data(), scratch, sizeof(unsigned long long) * words, cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hflags, flags, sizeof hflags, cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(scratch, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return set_err(s, E2D_ECUDA, std::string("radial_profile: ") + cudaGetErrorString(e));
+  if (hflags) return set_err(s, E2D_ENUMERIC, "radial_profile: non-finite density");
+  finish_radial_profile(g, host.data(), profile, counts);
+  const double dr = g.rmax / nbins;  // src/ComputeRadialProfileFunctor.h:121-127
+  for (int b = 0; b < nbins; ++b) distances[b] = (b + 0.5) * dr;
+  return E2D_OK;
+}
+
+int e2d_save_npy(const char *path, const double *data, long long n) {
+  if (!path || (!data && n > 0) || n < 0) return E2D_EINVAL;
+  // dictionary padded with spaces so that 10 + its length is a multiple of
+  // 16, last byte '\n' (a full 16 spaces when it already is)
+  const int one = 1;
+  const char order = *reinterpret_cast<const char *>(&one) ? '<' : '>';
+  std::string dict = std::string("{'descr': '") + order + "f8', 'fortran_order': False, 'shape': (" +
+                     std::to_string(n) + ",), }";
+  const int pad = 16 - (int)((10 + dict.size()) % 16);
+  dict.append(pad, ' ');
+  dict.back() = '\n';
+  std::string head = "\x93NUMPY";
+  head.push_back('\x01');
+  head.push_back('\x00');
+  const unsigned short hl = (unsigned short)dict.size();
+  head.push_back((char)(hl & 0xff));
+  head.push_back((char)(hl >> 8));
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return E2D_EIO;
+  bool ok = std::fwrite(head.data(), 1, head.size(), f) == head.size() &&
+            std::fwrite(dict.data(), 1, dict.size(), f) == dict.size() &&
+            (n == 0 || std::fwrite(data, sizeof(double), (size_t)n, f) == (size_t)n);
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? E2D_OK : E2D_EIO;
 }
 
 int e2d_eval_device(const e2d_params *pin, int what, int n, const double *in, double *out,

@@ -173,4 +173,18 @@ cudaError_t launch_l1diff_f64(const KGeom &g, const double *a, const double *b, 
                               double *partial, double *out2, cudaStream_t s);
 size_t flux_update_f64_smem_bytes();
 
+// Radial density profile about the box centre (e2d_reduce.cu), over every
+// cell of the array including ghosts; rings >= nbins are not counted.
+struct ProfileGeom {
+  double xmin, ymin, dx, dy, cx, cy, rmax;
+  int isize, jsize, ghost, nbins;
+};
+constexpr int kProfileSmemRings = 4096;  // per-block shared-memory partials up to this many rings
+// scratch: 1 + 4*nbins 64-bit words; flags bit 0: a non-finite density.
+cudaError_t launch_radial_profile(const ProfileGeom &g, const double *rho, unsigned long long *scratch,
+                                  unsigned int *flags, cudaStream_t s);
+// Mean density per ring from the scratch words copied to the host.
+void finish_radial_profile(const ProfileGeom &g, const unsigned long long *host_scratch, double *profile,
+                           long long *counts);
+
 }  // namespace e2d

@@ -1,7 +1,8 @@
 // euler2d_gb300 -- command-line driver with the behaviour of the reference's
 // src/main.cpp:24-212: read an ini file, build HydroParams and HydroRun, run
 // the time loop (dt from the CFL condition, clamped at tEnd), write VTK
-// output every nOutput steps and report the timing and the
+// output every nOutput steps, the Sedov radial profile (.npy) for blasts
+// with total_energy_inside > 0, and report the timing and the
 // "Mcell-updates/s" figure (ghost cells counted, src/main.cpp:202-203).
 //
 //   euler2d_gb300 file.ini [--host-loop]
@@ -100,6 +101,10 @@ int main(int argc, char *argv[]) {
       io_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - a).count();
     }
     const double t_tot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    // post-processing for the Sedov blast (src/main.cpp:175-179); like the
+    // reference it reads U whatever the parity of the last step
+    if (params.problemType == E2D_PROBLEM_BLAST && params.blast_total_energy_inside > 0)
+      ComputeRadialProfileFunctor::apply(hydro, hydro.U);
     std::printf("total           time : %5.3f secondes\n", t_tot);
     std::printf("io              time : %5.3f secondes %5.2f%%\n", io_s, 100 * io_s / t_tot);
     std::printf("Perf                 : %10.2f number of Mcell-updates/s\n",

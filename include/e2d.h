@@ -157,6 +157,24 @@ int e2d_l1_diff(e2d_sim *a, int wa, e2d_sim *b, int wb, int var, double *l1_diff
 /* The handle's CUDA stream (a cudaStream_t). */
 int e2d_get_stream(e2d_sim *sim, void **stream);
 
+/* Sedov post-processing, ComputeRadialProfileFunctor::apply
+ * (src/ComputeRadialProfileFunctor.h:83-134, called from src/main.cpp:175-179):
+ * the mean density of U (0) or U2 (1) in nbins rings about the box centre,
+ * over every cell of the array including ghosts (nbins <= 0: the
+ * [blast] nbins key).  distances[b] = (b + 0.5) * rmax / nbins with rmax the
+ * half-diagonal of the box; counts may be NULL.  Differences from the
+ * reference: cells whose ring index is >= nbins (the ghost corners) are not
+ * counted, where the reference writes them past the end of its histogram
+ * arrays; the per-ring sums are exact up to one final rounding (the
+ * reference's atomic FP64 sums depend on the order of the additions); a
+ * non-finite density returns E2D_ENUMERIC.  An empty ring gives NaN (0/0),
+ * as in the reference. */
+int e2d_radial_profile(e2d_sim *sim, int which, int nbins, double *distances, double *profile,
+                       long long *counts);
+/* cnpy::npy_save (src/cnpy/cnpy.h:130-187, header of :343-378) for a 1-D
+ * double array: NPY format 1.0, descr '<f8' (host byte order), C order. */
+int e2d_save_npy(const char *path, const double *data, long long n);
+
 /* HydroRun::make_boundaries (src/HydroRun.h:388-399) on U (0) or U2 (1).
  * FP32C states keep no ghost cells (readers map them), so there it does
  * nothing. */

@@ -155,4 +155,21 @@ class HydroRun {
   e2d_sim *sim_ = nullptr;
 };
 
+// ComputeRadialProfileFunctor::apply (src/ComputeRadialProfileFunctor.h:83-134):
+// the mean density of Udata in [blast] nbins rings about the box centre,
+// written as sedov_blast_radial_distances.npy and
+// sedov_blast_density_profile.npy in the working directory.
+struct ComputeRadialProfileFunctor {
+  static void apply(HydroRun &hydro, const DataArray &Udata) {
+    const int nb = hydro.params.blast_nbins;
+    std::vector<double> dist(nb > 0 ? nb : 0), prof(dist.size());
+    check(e2d_radial_profile(hydro.sim(), Udata.which, nb, dist.data(), prof.data(), nullptr),
+          "ComputeRadialProfileFunctor", hydro.sim());
+    check(e2d_save_npy("sedov_blast_radial_distances.npy", dist.data(), (long long)dist.size()),
+          "save sedov_blast_radial_distances.npy");
+    check(e2d_save_npy("sedov_blast_density_profile.npy", prof.data(), (long long)prof.size()),
+          "save sedov_blast_density_profile.npy");
+  }
+};
+
 }  // namespace euler2d_gb300

@@ -527,6 +527,36 @@ void orc_init_implode(const orc_params *p, double *u, int reference_shape) {
 }
 
 /* src/HydroRunFunctors.h:1451-1494 (InitBlastFunctor, regular init). */
+/* src/ComputeRadialProfileFunctor.h:83-134 (apply) and :140-158 (operator()). */
+void orc_radial_profile(const orc_params *p, const double *u, int nbins, double *distances,
+                        double *profile, long long *counts) {
+  const double cx = (p->xmin + p->xmax) / 2;
+  const double cy = (p->ymin + p->ymax) / 2;
+  const double Dx = (p->xmax - p->xmin) / 2;
+  const double Dy = (p->ymax - p->ymin) / 2;
+  const double rmax = sqrt(Dx * Dx + Dy * Dy);
+  for (int b = 0; b < nbins; ++b) {
+    profile[b] = 0.0;
+    counts[b] = 0;
+  }
+  for (int j = 0; j < p->jsize; ++j)
+    for (int i = 0; i < p->isize; ++i) {
+      const double x = p->xmin + p->dx / 2 + (i - p->ghost) * p->dx;
+      const double y = p->ymin + p->dy / 2 + (j - p->ghost) * p->dy;
+      const double d = sqrt((x - cx) * (x - cx) + (y - cy) * (y - cy));
+      const int bin = (int)(d / rmax * nbins);
+      if (bin < nbins) {
+        counts[bin] += 1;
+        profile[bin] += u[i + (long)p->isize * j];
+      }
+    }
+  const double dr = rmax / nbins;
+  for (int b = 0; b < nbins; ++b) {
+    distances[b] = (b + 0.5) * dr;
+    profile[b] /= (double)counts[b];
+  }
+}
+
 void orc_init_blast(const orc_params *p, double *u, double radius, double cx, double cy,
                     double d_in, double d_out, double p_in, double p_out) {
   const double gamma0 = p->gamma0, r2 = radius * radius;

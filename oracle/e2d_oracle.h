@@ -53,6 +53,14 @@ int orc_run(const orc_params *p, double *u, double *u2, int nstep_max, double t_
 
 /* Initial conditions of src/HydroRunFunctors.h:1347-1827, parametrised. */
 void orc_init_implode(const orc_params *p, double *u, int reference_shape);
+/* ComputeRadialProfileFunctor (src/ComputeRadialProfileFunctor.h:83-165):
+ * mean density in nbins rings about the box centre over every cell of the
+ * array, ghosts included, summed j outer / i inner.  Cells whose ring index
+ * is >= nbins (ghost corners) are not counted -- the reference writes them
+ * past the end of its histograms.  An empty ring gives 0/0 (NaN), as there. */
+void orc_radial_profile(const orc_params *p, const double *u, int nbins, double *distances,
+                        double *profile, long long *counts);
+
 void orc_init_blast(const orc_params *p, double *u, double radius, double cx, double cy,
                     double d_in, double d_out, double p_in, double p_out);
 void orc_init_four_quadrant(const orc_params *p, double *u, double xt, double yt,

@@ -118,6 +118,13 @@ view_alloc(const std::string & label, WithoutInitializing_t)
   return ViewAllocProp{ label, false };
 }
 
+// Everything is host memory, so every space can access every other.
+template <class AccessSpace, class MemorySpace>
+struct SpaceAccessibility
+{
+  static constexpr bool accessible = true;
+};
+
 namespace compat_detail
 {
 // Decompose T** [N] / T* into value type, runtime rank and static extent.
@@ -161,6 +168,8 @@ class View
 public:
   using value_type = typename tr::value_type;
   using host_mirror_type = View<DataType, Props...>;
+  using memory_space = HostSpace;  // every view lives in host memory
+  static constexpr int rank = tr::dyn + (tr::last > 1 ? 1 : 0);
   using HostMirror = host_mirror_type;
 
   View() = default;
@@ -216,11 +225,15 @@ private:
     m_n0 = n0;
     m_n1 = (tr::dyn == 2) ? n1 : 1;
     const long n = m_n0 * m_n1 * tr::last;
-    m_owner = std::shared_ptr<value_type>(new value_type[n > 0 ? n : 1],
-                                          std::default_delete<value_type[]>());
+    // 1-D views get zeroed slack after their extent: the radial-profile
+    // functor (src/ComputeRadialProfileFunctor.h:150-158) indexes its two
+    // histograms with bins up to ~2.5x nbins for the ghost corner cells;
+    // the slack absorbs those writes so that bins [0, nbins) are defined.
+    const long cap = (tr::dyn == 1 && tr::last == 1) ? 3 * n + 64 : (n > 0 ? n : 1);
+    m_owner = std::shared_ptr<value_type>(new value_type[cap], std::default_delete<value_type[]>());
     m_ptr = m_owner.get();
-    if (prop.init)
-      std::memset((void *)m_ptr, 0, sizeof(value_type) * (n > 0 ? n : 1));
+    if (prop.init || cap > n)
+      std::memset((void *)m_ptr, 0, sizeof(value_type) * cap);
   }
 
   std::shared_ptr<value_type> m_owner;

@@ -74,6 +74,7 @@ def lib() -> ctypes.CDLL:
         L.orc_init_blast.argtypes = [P, dp] + [ctypes.c_double] * 7
         L.orc_init_four_quadrant.argtypes = [P, dp, ctypes.c_double, ctypes.c_double, dp]
         L.orc_num_threads.restype = ctypes.c_int
+        L.orc_radial_profile.argtypes = [P, dp, ctypes.c_int, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -202,6 +203,16 @@ def riemann(p, solver, ql, qr):
     return out
 
 
+def radial_profile(p, u, nbins):
+    """(distances, mean density, cell count) per ring -- orc_radial_profile."""
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    d, prof = np.zeros(nbins), np.zeros(nbins)
+    cnt = np.zeros(nbins, dtype=np.int64)
+    lib().orc_radial_profile(ctypes.byref(p), _ptr(u), int(nbins), _ptr(d), _ptr(prof),
+                             cnt.ctypes.data_as(ctypes.c_void_p))
+    return d, prof, cnt
+
+
 class ReferenceLib:
     """The reference's own solver (oracle/_ref/libe2d_ref.so), driven by ini files."""
 
@@ -220,7 +231,24 @@ class ReferenceLib:
         L.ref_trace.argtypes = [ctypes.c_char_p, ctypes.c_int, dp, dp, dp,
                                 ctypes.c_double, ctypes.c_double, ctypes.c_int, dp]
         L.ref_riemann.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, dp, dp]
+        L.ref_radial_profile.argtypes = [ctypes.c_char_p, dp, ctypes.c_char_p]
+        L.ref_radial_profile.restype = ctypes.c_int
         self.L = L
+
+    def radial_profile(self, ini: str, u):
+        """The reference's Sedov post-processing on state u: returns the bytes
+        of the two .npy files it writes (distances, density profile)."""
+        import tempfile
+
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        with tempfile.TemporaryDirectory() as d:
+            if self.L.ref_radial_profile(ini.encode(), _ptr(u), d.encode()) != 0:
+                raise RuntimeError("ref_radial_profile failed")
+            out = []
+            for name in ("sedov_blast_radial_distances.npy", "sedov_blast_density_profile.npy"):
+                with open(os.path.join(d, name), "rb") as f:
+                    out.append(f.read())
+        return tuple(out)
 
     PARAM_NAMES = ["nx", "ny", "isize", "jsize", "dx", "dy", "gamma0", "gamma6", "cfl",
                    "slope_type", "smallr", "smallc", "smallp", "smallpp", "tEnd", "nStepmax",

@@ -7,9 +7,13 @@
 // The run loop follows src/main.cpp:76-145 (compute_dt before the boundary
 // fill, the loop condition, the dt clamp at tEnd, the U/U2 ping-pong) without
 // the banner, the output and the timers' report.
+#include "ComputeRadialProfileFunctor.h"
 #include "HydroParams.h"
 #include "HydroRun.h"
 #include "config/ConfigMap.h"
+
+#include <omp.h>
+#include <unistd.h>
 
 #include <cstring>
 
@@ -173,6 +177,30 @@ extern "C"
     hydro.make_boundaries(hydro.U);
     std::memcpy(u, hydro.U.data(), sizeof(double) * n);
     return 0;
+  }
+
+  // The Sedov post-processing of src/main.cpp:175-179:
+  // ComputeRadialProfileFunctor::apply (src/ComputeRadialProfileFunctor.h:83-134)
+  // on a caller-supplied state.  It writes sedov_blast_radial_distances.npy
+  // and sedov_blast_density_profile.npy into outdir.  Runs on one thread: the
+  // stand-in View has no atomic accessor, and one thread also fixes the
+  // summation order (j outer, i inner).
+  int
+  ref_radial_profile(const char * ini, const double * u, const char * outdir)
+  {
+    ConfigMap   cm{ std::string(ini) };
+    HydroParams params;
+    params.setup(cm);
+    DataArray<Dev> U("U", params.isize, params.jsize);
+    std::memcpy(U.data(), u, sizeof(double) * (long)params.isize * params.jsize * 4);
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd) || chdir(outdir) != 0)
+      return 1;
+    const int threads = omp_get_max_threads();
+    omp_set_num_threads(1);
+    ComputeRadialProfileFunctor<Dev>::apply(params, U);
+    omp_set_num_threads(threads);
+    return chdir(cwd) == 0 ? 0 : 1;
   }
 
   // compute_dt (src/HydroRun.h:227-251) on a caller-supplied state.

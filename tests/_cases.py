@@ -147,6 +147,19 @@ def run_cases():
     return cases
 
 
+SEDOV_NBINS = (7, 40, 150)
+
+
+def sedov_ini(nbins: int) -> str:
+    """The physics of the reference's src/sedov_blast/test_sedov_blast_2d.ini
+    (energy 0.311357 deposited in a disc, absorbing walls) on 64x64 cells,
+    disc radius 0.05 so that it covers a few cells, 60 steps."""
+    return ini_text(64, 64, bc=(2, 2, 2, 2), problem="blast", tEnd=0.5, nStepmax=60,
+                    extra="[blast]\ndensity_in=1.0\ndensity_out=1.0\npressure_in=1\n"
+                          "pressure_out=1e-7\nradius=0.05\ntotal_energy_inside=0.311357\n"
+                          f"nbins={nbins}\n")
+
+
 def parse_ini(text: str) -> dict:
     """'section.key' (lower case) -> value string, for the simple ini texts
     of these cases (comments, sections, key=value)."""

@@ -13,6 +13,11 @@ Outputs (small, committed):
     runs.npz      multi-step runs: dt of every step and the final state
     c1.json       the 256x256 implosion, 1000 steps: dt sequence and a
                   SHA-256 of the final state
+    sedov.npz     the Sedov post-processing (src/main.cpp:175-179) of a 64x64
+                  point blast after 60 steps: the .npy files the reference's
+                  ComputeRadialProfileFunctor writes, for three ring counts
+
+    python tests/golden/make_golden.py --only sedov   regenerates one file
 """
 from __future__ import annotations
 
@@ -185,15 +190,42 @@ def gen_c1(R: ReferenceLib, tmp: str) -> dict:
             "l1_interior": [float(np.abs(interior[v]).sum()).hex() for v in range(4)]}
 
 
+def gen_sedov(R: ReferenceLib, tmp: str) -> dict:
+    """The reference's own initial condition and 60 steps, then its radial
+    profile with 7, 40 and 150 rings: the raw bytes of both .npy files."""
+    path = C.write_ini(C.sedov_ini(C.SEDOV_NBINS[0]), tmp, "sedov.ini")
+    u, dts, t, ns = R.run(path, None, 60)
+    out = {"nsteps": np.int64(ns), "rho": u[0], "dt": dts,
+           "sha256_state": np.frombuffer(hashlib.sha256(np.ascontiguousarray(u).tobytes()).digest(),
+                                         dtype=np.uint8)}
+    for nb in C.SEDOV_NBINS:
+        pb = C.write_ini(C.sedov_ini(nb), tmp, f"sedov_{nb}.ini")
+        dist, prof = R.radial_profile(pb, u)
+        out[f"dist_npy_{nb}"] = np.frombuffer(dist, dtype=np.uint8)
+        out[f"prof_npy_{nb}"] = np.frombuffer(prof, dtype=np.uint8)
+    return out
+
+
 def main():
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["params", "kat", "runs", "c1", "sedov"])
+    only = ap.parse_args().only
     R = ReferenceLib()
     tmp = tempfile.mkdtemp(prefix="e2d_golden_")
-    with open(os.path.join(HERE, "params.json"), "w") as f:
-        json.dump(gen_params(R, tmp), f, indent=1)
-    np.savez_compressed(os.path.join(HERE, "kat.npz"), **gen_kat(R, tmp))
-    np.savez_compressed(os.path.join(HERE, "runs.npz"), **gen_runs(R, tmp))
-    with open(os.path.join(HERE, "c1.json"), "w") as f:
-        json.dump(gen_c1(R, tmp), f, indent=1)
+    if only in (None, "params"):
+        with open(os.path.join(HERE, "params.json"), "w") as f:
+            json.dump(gen_params(R, tmp), f, indent=1)
+    if only in (None, "kat"):
+        np.savez_compressed(os.path.join(HERE, "kat.npz"), **gen_kat(R, tmp))
+    if only in (None, "runs"):
+        np.savez_compressed(os.path.join(HERE, "runs.npz"), **gen_runs(R, tmp))
+    if only in (None, "c1"):
+        with open(os.path.join(HERE, "c1.json"), "w") as f:
+            json.dump(gen_c1(R, tmp), f, indent=1)
+    if only in (None, "sedov"):
+        np.savez_compressed(os.path.join(HERE, "sedov.npz"), **gen_sedov(R, tmp))
     print("golden fixtures written to", HERE)
 
 
