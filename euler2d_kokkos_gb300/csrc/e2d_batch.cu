@@ -88,7 +88,7 @@ int size_class_of(int nx, int ny) {
 
 struct e2d_batch {
   int riemann = E2D_RIEMANN_HLLC;
-  int variant = 1;
+  int variant = 2;
   int strip_h[3] = {16, 32, 64};  // per size class
   cudaStream_t stream = nullptr;
   char *pool = nullptr;
@@ -140,14 +140,32 @@ int sync_mirrors(e2d_batch *b) {
 }
 
 // The work list: used, active instances; each gets the strip height of its
-// size class.
+// size class, lowered (to 16 rows at least) while the list has fewer strips
+// than the grid has warps -- the tail of a batch, when a few large instances
+// are left, would otherwise leave SMs idle.  Results do not depend on it.
 int rebuild_list(e2d_batch *b) {
   std::vector<int> list, begin;
+  const int per_sm = batch_blocks_per_sm(b->riemann, b->variant);
+  const long long warps = 152LL * per_sm * 4;
+  int shift = 0;
+  for (;; ++shift) {
+    long long n = 0;
+    bool all_min = true;
+    for (int k = 0; k < b->max_inst; ++k) {
+      HostInst &h = b->slots[k];
+      if (!h.used || !h.mirror.active) continue;
+      KParams32 kp = h.mirror.kp;
+      kp.strip_h = std::max(16, ((b->strip_h[h.size_class] >> shift) / 16) * 16);
+      all_min &= kp.strip_h == 16;
+      n += strips_of(kp);
+    }
+    if (n >= warps || all_min) break;
+  }
   int total = 0;
   for (int k = 0; k < b->max_inst; ++k) {
     HostInst &h = b->slots[k];
     if (!h.used || !h.mirror.active) continue;
-    const int sh = b->strip_h[h.size_class];
+    const int sh = std::max(16, ((b->strip_h[h.size_class] >> shift) / 16) * 16);
     if (h.mirror.kp.strip_h != sh) {
       h.mirror.kp.strip_h = sh;
       h.mirror.nstrips = strips_of(h.mirror.kp);
@@ -170,7 +188,6 @@ int rebuild_list(e2d_batch *b) {
   B_CK(b, cudaStreamSynchronize(b->stream), "list sync");
   b->list = list;
   b->total_strips = total;
-  const int per_sm = batch_blocks_per_sm(b->riemann, b->variant);
   b->grid = std::max(1, std::min((total + 3) / 4, 152 * per_sm));
   drop_graphs(b);
   b->list_dirty = false;
@@ -422,11 +439,11 @@ int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_used) {
 
 int e2d_batch_set_tuning(e2d_batch *b, int variant, const int strip_h[3]) {
   if (!b) return E2D_EINVAL;
-  if (variant == 0 || variant == 1) b->variant = variant;
+  if (variant >= 0 && variant <= 3) b->variant = variant;
   // strip heights are whole CFL fold units (16 rows)
   if (strip_h)
     for (int c = 0; c < 3; ++c)
-      if (strip_h[c] > 0 && strip_h[c] <= 1024) b->strip_h[c] = (strip_h[c] + 15) / 16 * 16;
+      if (strip_h[c] > 0 && strip_h[c] <= 512) b->strip_h[c] = (strip_h[c] + 15) / 16 * 16;
   b->list_dirty = true;
   return E2D_OK;
 }
@@ -482,7 +499,7 @@ int e2d_batch_autotune(e2d_batch *b, int iters_per_trial) {
   // register budget first, then each size class's strip height
   double best_ms = 1e30;
   int best_v = b->variant;
-  for (int v = 0; v < 2 && rc == E2D_OK; ++v) {
+  for (int v = 0; v < 4 && rc == E2D_OK; ++v) {
     b->variant = v;
     double ms;
     rc = trial(&ms);

@@ -256,7 +256,7 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
   if (const char *v = std::getenv("E2D_F32C_VARIANT")) s->kp32.variant = std::atoi(v);
   // strip heights are whole 16-row CFL fold units
   if (const char *v = std::getenv("E2D_F32C_STRIP_H"))
-    if (std::atoi(v) > 0) s->kp32.strip_h = (std::atoi(v) + 15) / 16 * 16;
+    if (std::atoi(v) > 0 && std::atoi(v) <= 512) s->kp32.strip_h = (std::atoi(v) + 15) / 16 * 16;
   auto fail = [&](int status) {
     e2d_destroy(s);
     return status;

@@ -258,21 +258,14 @@ __device__ __forceinline__ float2 cfl_term2(const C2 &k, float2 idx, const float
   return fma2(c + abs2(q[E2D_IU]), f2(idx.x), (c + abs2(q[E2D_IV])) * f2(idx.y));
 }
 
-// Warp arg-max of an FP32 term, then lane 0 folds the winner's FP64 term
-// into *target -- skipped when the FP32 term is more than 1e-4 below the
-// running maximum (FP32 terms are within ~1e-6 of the FP64 ones, so such a
-// cell cannot raise the maximum).
-__device__ __forceinline__ void warp_cfl_fold(const KParams32 &kp, float term, long long cell,
-                                              const float *w, unsigned long long *target,
-                                              unsigned int *status) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const float ot = __shfl_xor_sync(0xffffffffu, term, off);
-    const long long oc = __shfl_xor_sync(0xffffffffu, cell, off);
-    if (ot > term || (ot == term && oc > cell)) term = ot, cell = oc;
-  }
-  __syncwarp();  // the winner was written by a lane of this warp
-  if ((threadIdx.x & 31) != 0 || cell < 0) return;
+// Folds one candidate's FP64 CFL term into *target -- skipped when its FP32
+// term is more than 1e-4 below the running maximum (FP32 terms are within
+// ~1e-6 of the FP64 ones, so such a cell cannot hold the maximum; any value
+// of the running maximum is a lower bound of the final one, so the final
+// maximum does not depend on which candidates were skipped).
+__device__ __forceinline__ void fold_candidate(const KParams32 &kp, float term, long long cell,
+                                               const float *w, unsigned long long *target,
+                                               unsigned int *status) {
   const double cur = __longlong_as_double((long long)(*(volatile unsigned long long *)target));
   if ((double)term < cur * (1.0 - 1e-4)) return;
   const long long P = kp.wplane;
@@ -284,6 +277,35 @@ __device__ __forceinline__ void warp_cfl_fold(const KParams32 &kp, float term, l
     atomicMax(target, (unsigned long long)__double_as_longlong(t64));
   else
     atomicOr(status, nonfinite64(t64) ? (unsigned)E2D_FLAG_NONFINITE : (unsigned)E2D_FLAG_BAD_DT);
+}
+
+// Warp arg-max of an FP32 term (ties to the larger cell), then lane 0 folds
+// the winner.
+__device__ __forceinline__ void warp_cfl_fold(const KParams32 &kp, float term, long long cell,
+                                              const float *w, unsigned long long *target,
+                                              unsigned int *status) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float ot = __shfl_xor_sync(0xffffffffu, term, off);
+    const long long oc = __shfl_xor_sync(0xffffffffu, cell, off);
+    if (ot > term || (ot == term && oc > cell)) term = ot, cell = oc;
+  }
+  __syncwarp();  // the winner was written by a lane of this warp
+  if ((threadIdx.x & 31) != 0 || cell < 0) return;
+  fold_candidate(kp, term, cell, w, target, status);
+}
+
+// The same arg-max for a fold unit inside a strip march, with two warp
+// reductions: `local` is the lane's best cell as its index in the strip,
+// (row - rb) * 64 + (column - (cb - 2)), plus one (0: no candidate), which
+// orders cells as their array offsets do.  CFL terms of valid cells are
+// positive, so their bit patterns order like their values.
+__device__ __forceinline__ int unit_argmax(float best, int local, float *term) {
+  const unsigned int tb = local > 0 ? __float_as_uint(best) : 0u;
+  const unsigned int m = __reduce_max_sync(0xffffffffu, tb);
+  const unsigned int win = __reduce_max_sync(0xffffffffu, (m != 0u && tb == m) ? (unsigned int)local : 0u);
+  *term = __uint_as_float(m);
+  return (int)win;
 }
 
 // ------------------------------------------------------------ conversions
@@ -387,15 +409,20 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
 // state is folded into *target once per fold unit -- the strip's 60 output
 // columns by 16 rows of the interior -- so that the set of FP64-recomputed
 // candidates depends only on the grid, never on the strip height, the
-// kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS).
+// kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
+// most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
+// parked winners are recomputed in FP64 together when the strip ends.
 template <int RS>
 __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
                                             unsigned int *status) {
-  float best = -1.0f;
-  long long bcell = -1;
+  float best = -1.0f;      // the lane's largest CFL term in the current fold unit
+  int blocal = 0;          // and its strip-local index + 1 (0: none)
+  float pend_term = 0.0f;  // lane u: the winner of the strip's fold unit u
+  int pend_local = 0;
+  int unit = 0;
   const KGeom &g = kp.g;
   const KPhys<float> &ph = kp.ph;
   const int SH = kp.strip_h;
@@ -537,15 +564,19 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
         }
         if (target) {
           const float2 t = cfl_term2(k, idx, nh);
-          if (t.x > best) best = t.x, bcell = base;
-          if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, bcell = base + 1;
+          const int loc = (m - 1 - rb) * 64 + 2 * lane + 1;
+          if (t.x > best) best = t.x, blocal = loc;
+          if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, blocal = loc + 1;
         }
       }
       const int r = m - 1;
       if (target && (((r - 2) % CFL_UNIT_ROWS) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
-        warp_cfl_fold(kp, best, bcell, w_out, target, status);
+        float ut;
+        const int win = unit_argmax(best, blocal, &ut);
+        if (lane == unit) pend_term = ut, pend_local = win;
+        ++unit;
         best = -1.0f;
-        bcell = -1;
+        blocal = 0;
       }
     }
     // roll
@@ -556,6 +587,15 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       ymax_prev[v] = ymax[v];
       fx_prev[v] = fx[v];
       fy_prev[v] = fy[v];
+    }
+  }
+  // the strip's fold-unit winners, one lane each, folded in parallel
+  if (target) {
+    __syncwarp();  // the winners were written by lanes of this warp
+    if (pend_local > 0) {
+      const int L = pend_local - 1;
+      const long long cell = (long long)kp.wpitch * (rb + L / 64) + (cb - 2) + (L % 64);
+      fold_candidate(kp, pend_term, cell, w_out, target, status);
     }
   }
 }
@@ -728,10 +768,12 @@ cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const 
                               const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
                               cudaStream_t s) {
   if (n_inst <= 0 || total_strips <= 0) return cudaSuccess;
-  if (variant == 0)
-    launch_batch_minb<1>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s);
-  else
-    launch_batch_minb<4>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s);
+  switch (variant) {
+    case 0: launch_batch_minb<1>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
+    case 2: launch_batch_minb<3>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
+    case 3: launch_batch_minb<2>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
+    default: launch_batch_minb<4>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
+  }
   return cudaGetLastError();
 }
 
@@ -740,25 +782,25 @@ cudaError_t launch_batch_arm(BatchInst *inst, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-int batch_blocks_per_sm(int riemann, int variant) {
+template <int RS>
+static int batch_occupancy(int variant) {
   int n = 0;
   cudaError_t e;
-  const bool v0 = variant == 0;
-  switch (riemann) {
-    case E2D_RIEMANN_HLLC:
-      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLLC, 1>, NT, 0)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLLC, 4>, NT, 0);
-      break;
-    case E2D_RIEMANN_HLL:
-      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLL, 1>, NT, 0)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_HLL, 4>, NT, 0);
-      break;
-    default:
-      e = v0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_APPROX, 1>, NT, 0)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<E2D_RIEMANN_APPROX, 4>, NT, 0);
-      break;
+  switch (variant) {
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 1>, NT, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3>, NT, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 2>, NT, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4>, NT, 0); break;
   }
   return (e == cudaSuccess && n > 0) ? n : 1;
+}
+
+int batch_blocks_per_sm(int riemann, int variant) {
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC: return batch_occupancy<E2D_RIEMANN_HLLC>(variant);
+    case E2D_RIEMANN_HLL: return batch_occupancy<E2D_RIEMANN_HLL>(variant);
+    default: return batch_occupancy<E2D_RIEMANN_APPROX>(variant);
+  }
 }
 
 // Rows per warp strip: the largest of 64, 32, 16 that still gives every SM
@@ -782,7 +824,7 @@ void make_kparams32(const e2d_params &p, KParams32 *kp) {
                         (float)d.gm1, (float)d.entho, (float)d.smallc2, (float)d.dx, (float)d.dy};
   kp->wpitch = (p.isize + 3) & ~3;
   kp->wplane = (long long)kp->wpitch * p.jsize;
-  kp->variant = 1;
+  kp->variant = 2;  // at least 3 blocks per SM: 166 registers, no spills (fastest at 8192^2)
   kp->strip_h = default_strip_h(p.nx, p.ny);
 }
 
@@ -836,12 +878,15 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
   const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
   const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
   const int blocks = (nsx * nsy + WPB - 1) / WPB;
-  // register budget variant: 0 -> as many registers as the code wants
-  // (3 blocks per SM), 1 -> 128 registers (4 blocks per SM, small spill)
-  if (kp.variant == 0)
-    launch_step_minb<1>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s);
-  else
-    launch_step_minb<4>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s);
+  // register budget variant (minimum resident blocks of 128 threads per SM):
+  // 0 -> 1 (as many registers as the code wants), 1 -> 4 (128 registers),
+  // 2 -> 3 (168 registers), 3 -> 2
+  switch (kp.variant) {
+    case 0: launch_step_minb<1>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 2: launch_step_minb<3>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 3: launch_step_minb<2>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    default: launch_step_minb<4>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+  }
   return cudaGetLastError();
 }
 

@@ -251,9 +251,10 @@ int e2d_batch_release(e2d_batch *b, int id);
 int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_instances);
 /* The batch's CUDA stream (a cudaStream_t). */
 int e2d_batch_stream(e2d_batch *b, void **stream);
-/* Tuning: register-budget variant of the batch kernel (0 or 1) and rows per
- * strip for the size classes max(nx, ny) <= 192, <= 512, > 512.  Results do
- * not depend on them.  e2d_batch_autotune times the candidates on the live
+/* Tuning: register-budget variant of the batch kernel (0..3: at least 1, 4,
+ * 3 or 2 resident blocks of 128 threads per SM) and rows per strip (16..512,
+ * rounded up to a multiple of 16) for the size classes max(nx, ny) <= 192,
+ * <= 512, > 512.  Results do not depend on them.  e2d_batch_autotune times the candidates on the live
  * batch (its iterations advance the instances) and keeps the fastest. */
 int e2d_batch_set_tuning(e2d_batch *b, int variant, const int strip_h[3]);
 int e2d_batch_get_tuning(const e2d_batch *b, int *variant, int strip_h[3]);
