@@ -404,6 +404,47 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
   if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
 }
 
+// Shared-memory row ring of the staged march: each warp copies the rows it
+// will need PF_DIST iterations ahead with cp.async (no registers held while
+// the copies fly); a slot holds the 8 planes (hi, lo) x 64 columns of one
+// row, each lane copying and later reading only its own two columns.
+constexpr int PF_DIST = 2;                 // rows copied ahead of their use
+constexpr int RING = PF_DIST + 3;          // rows m-1 .. m+1+PF_DIST
+constexpr int SLOT = 8 * 64;               // floats per slot
+constexpr int RING_FLOATS = WPB * RING * SLOT;
+
+__device__ __forceinline__ void cp_async8(float *dst, const float *src) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Copies array row r (ghost rows through the boundary map) for the lane's two
+// columns into `slot`; `direct`: both columns interior and read as a pair,
+// else columns s0, s1 (the boundary map of c0, c0 + 1).
+__device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__restrict__ w, int r, int c0,
+                                          bool direct, int s0, int s1, float *slot) {
+  const KGeom &g = kp.g;
+  bool fv;
+  const int sr = ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
+  const float *row = w + (long long)sr * kp.wpitch;
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    if (direct) {
+      cp_async8(slot + v * 64, row + v * kp.wplane + c0);
+    } else {
+      cp_async4(slot + v * 64, row + v * kp.wplane + s0);
+      cp_async4(slot + v * 64 + 1, row + v * kp.wplane + s1);
+    }
+  }
+}
+
 // One warp marches strip (sx, sy) of an instance: rows rb-2 .. re+1 are
 // read, rows rb .. re-1 written.  With a target, the CFL term of the new
 // state is folded into *target once per fold unit -- the strip's 60 output
@@ -412,12 +453,12 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
 // kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
-template <int RS>
+template <int RS, bool STAGED>
 __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
-                                            unsigned int *status) {
+                                            unsigned int *status, float *ring) {
   float best = -1.0f;      // the lane's largest CFL term in the current fold unit
   int blocal = 0;          // and its strip-local index + 1 (0: none)
   float pend_term = 0.0f;  // lane u: the winner of the strip's fold unit u
@@ -442,8 +483,39 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   float2 fy_prev[4];    // y-flux of the face between rows m-2 and m-1
 #pragma unroll
   for (int v = 0; v < 4; ++v) ymax_prev[v] = fx_prev[v] = fy_prev[v] = f2(0.0f);
-  float2 pf[4];  // conserved hi of row m+1, loaded one iteration ahead
-  {
+  float2 pf[4];  // (register path) conserved hi of row m+1, loaded one iteration ahead
+  // (staged path) the boundary map of the lane's columns and its ring slots
+  bool f0 = false, f1 = false;
+  int s0 = c0, s1 = c0 + 1;
+  if (STAGED && !direct) {
+    s0 = ghost_source(min(max(c0, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f0);
+    s1 = ghost_source(min(max(c0 + 1, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f1);
+  }
+  float *const lane_ring = ring + 2 * lane;
+  // hi of a staged row, ghost flips applied
+  auto staged_hi = [&](int r, float2 out[4]) {
+    const float *sl = lane_ring + ((r - rb + 2) % RING) * SLOT;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
+    if (f0) out[E2D_IU].x = -out[E2D_IU].x;
+    if (f1) out[E2D_IU].y = -out[E2D_IU].y;
+    bool fv;
+    ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
+    if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
+  };
+  if (STAGED) {
+    // rows rb-2 .. rb+PF_DIST-1, one commit group each
+    for (int r = rb - 2; r < rb + PF_DIST; ++r) {
+      stage_row(kp, w_in, r, c0, direct, s0, s1, lane_ring + ((r - rb + 2) % RING) * SLOT);
+      cp_async_commit();
+    }
+    cp_async_wait<PF_DIST>();
+    float2 u[4];
+    staged_hi(rb - 2, u);
+    prims2(k, u[0], u[1], u[2], u[3], qa);
+    staged_hi(rb - 1, u);
+    prims2(k, u[0], u[1], u[2], u[3], qb);
+  } else {
     float2 u[4];
     load_row(kp, w_in, rb - 2, c0, direct, u);
     prims2(k, u[0], u[1], u[2], u[3], qa);
@@ -455,7 +527,16 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   // (m-1|m); update of row m-1
   for (int m = rb - 1; m <= re; ++m) {
     float2 qc[4];
-    {
+    if (STAGED) {
+      // copy row m+1+PF_DIST (its slot last held row m-2), then wait for row m+1
+      const int rn = m + 1 + PF_DIST;
+      if (rn <= re + 1) stage_row(kp, w_in, rn, c0, direct, s0, s1, lane_ring + ((rn - rb + 2) % RING) * SLOT);
+      cp_async_commit();
+      cp_async_wait<PF_DIST>();
+      float2 u[4];
+      staged_hi(m + 1, u);
+      prims2(k, u[0], u[1], u[2], u[3], qc);
+    } else {
       float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
       // issue the next row's loads before this row's arithmetic
       if (m + 2 <= re + 1) load_row(kp, w_in, m + 2, c0, direct, pf);
@@ -465,7 +546,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     const bool upd = (m >= rb + 1) && writer;
     const long long ubase = c0 + (long long)kp.wpitch * (m - 1);
     float2 uhi[4], ulo[4];
-    if (upd) {
+    if (!STAGED && upd) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         uhi[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + v * kp.wplane));
@@ -545,6 +626,15 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       for (int v = 0; v < 4; ++v) fxl[v] = make_float2(__shfl_up_sync(0xffffffffu, fx_prev[v].y, 1), fx_prev[v].x);
       if (upd) {
         const long long base = ubase;
+        if (STAGED) {
+          // row m-1 is interior: its slot holds it unflipped
+          const float *sl = lane_ring + ((m - 1 - rb + 2) % RING) * SLOT;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            uhi[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
+            ulo[v] = *reinterpret_cast<const float2 *>(sl + (4 + v) * 64);
+          }
+        }
         float2 nh[4];
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
@@ -600,10 +690,11 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   }
 }
 
-template <int RS, int MINB>
+template <int RS, int MINB, bool STAGED>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
                 DevClock *clk, const int use_clock, const double host_dt) {
+  __shared__ __align__(16) float ring[STAGED ? RING_FLOATS : 4];
   const KGeom &g = kp.g;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -640,8 +731,9 @@ __global__ void __launch_bounds__(NT, MINB)
   const int nsy = (g.ny + SH - 1) / SH;
   const int strip = blockIdx.x * WPB + (tid >> 5);
   if (strip < nsx * nsy)
-    march_strip<RS>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
-                    use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status);
+    march_strip<RS, STAGED>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
+                            use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status,
+                            ring + (STAGED ? (tid >> 5) * RING * SLOT : 0));
   if (!use_clock) return;
 
   // the last block to finish advances the loop state (src/main.cpp:139-143)
@@ -694,10 +786,11 @@ __device__ __forceinline__ void batch_finalize(BatchInst &I) {
 // instance's own dt, folds the instance's next CFL maximum, and the last
 // strip of each instance advances that instance's loop state.  Results of an
 // instance do not depend on the other instances in the batch.
-template <int RS, int MINB>
+template <int RS, int MINB, bool STAGED>
 __global__ void __launch_bounds__(NT, MINB)
     k_batch_f32c(BatchInst *__restrict__ insts, const int *__restrict__ list_slots,
                  const int *__restrict__ strip_begin, const int n_inst, const int total_strips) {
+  __shared__ __align__(16) float ring[STAGED ? RING_FLOATS : 4];
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * WPB;
   for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < total_strips; w += nwarps) {
@@ -715,8 +808,9 @@ __global__ void __launch_bounds__(NT, MINB)
     const KParams32 &kp = I.kp;
     const int par = I.par;
     const int strip = w - strip_begin[lo];
-    march_strip<RS>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx, strip / I.nsx,
-                    lane, &I.acc[(I.nstep + 1) & 1], &I.status);
+    march_strip<RS, STAGED>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
+                            strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
+                            ring + (STAGED ? (threadIdx.x >> 5) * RING * SLOT : 0));
     if (lane == 0) {
       __threadfence();
       const unsigned int ticket = atomicAdd(&I.done, 1u);
@@ -748,18 +842,18 @@ int strips_of(const KParams32 &kp) {
   return nsx * ((kp.g.ny + kp.strip_h - 1) / kp.strip_h);
 }
 
-template <int MINB>
-static void launch_batch_minb(int riemann, BatchInst *insts, const int *slots, const int *sb, int n,
-                              int total, int grid, cudaStream_t s) {
+template <int MINB, bool STAGED>
+static void launch_batch_v(int riemann, BatchInst *insts, const int *slots, const int *sb, int n, int total,
+                           int grid, cudaStream_t s) {
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_batch_f32c<E2D_RIEMANN_HLLC, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLLC, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
       break;
     case E2D_RIEMANN_HLL:
-      k_batch_f32c<E2D_RIEMANN_HLL, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLL, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
       break;
     default:
-      k_batch_f32c<E2D_RIEMANN_APPROX, MINB><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_APPROX, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
       break;
   }
 }
@@ -768,11 +862,14 @@ cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const 
                               const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
                               cudaStream_t s) {
   if (n_inst <= 0 || total_strips <= 0) return cudaSuccess;
+  const int *ls = list_slots, *sb = strip_begin;
   switch (variant) {
-    case 0: launch_batch_minb<1>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
-    case 2: launch_batch_minb<3>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
-    case 3: launch_batch_minb<2>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
-    default: launch_batch_minb<4>(riemann, insts, list_slots, strip_begin, n_inst, total_strips, grid_blocks, s); break;
+    case 0: launch_batch_v<1, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
+    case 2: launch_batch_v<3, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
+    case 3: launch_batch_v<2, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
+    case 4: launch_batch_v<3, true>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
+    case 5: launch_batch_v<4, true>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
+    default: launch_batch_v<4, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
   }
   return cudaGetLastError();
 }
@@ -787,10 +884,12 @@ static int batch_occupancy(int variant) {
   int n = 0;
   cudaError_t e;
   switch (variant) {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 1>, NT, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3>, NT, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 2>, NT, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4>, NT, 0); break;
+    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 1, false>, NT, 0); break;
+    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3, false>, NT, 0); break;
+    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 2, false>, NT, 0); break;
+    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3, true>, NT, 0); break;
+    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4, true>, NT, 0); break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4, false>, NT, 0); break;
   }
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
@@ -824,7 +923,7 @@ void make_kparams32(const e2d_params &p, KParams32 *kp) {
                         (float)d.gm1, (float)d.entho, (float)d.smallc2, (float)d.dx, (float)d.dy};
   kp->wpitch = (p.isize + 3) & ~3;
   kp->wplane = (long long)kp->wpitch * p.jsize;
-  kp->variant = 2;  // at least 3 blocks per SM: 166 registers, no spills (fastest at 8192^2)
+  kp->variant = 4;  // 3 blocks per SM, rows staged by cp.async (fastest at 8192^2)
   kp->strip_h = default_strip_h(p.nx, p.ny);
 }
 
@@ -857,18 +956,18 @@ cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, i
   return launch_f32c_dt_to(kp, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status, s);
 }
 
-template <int MINB>
-static void launch_step_minb(const KParams32 &kp, int riemann, int blocks, const float *w_in, float *w_out,
-                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
+template <int MINB, bool STAGED>
+static void launch_step_v(const KParams32 &kp, int riemann, int blocks, const float *w_in, float *w_out,
+                          DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_step_f32c<E2D_RIEMANN_HLLC, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLLC, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     case E2D_RIEMANN_HLL:
-      k_step_f32c<E2D_RIEMANN_HLL, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLL, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     default:
-      k_step_f32c<E2D_RIEMANN_APPROX, MINB><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_APPROX, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
   }
 }
@@ -878,14 +977,17 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
   const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
   const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
   const int blocks = (nsx * nsy + WPB - 1) / WPB;
-  // register budget variant (minimum resident blocks of 128 threads per SM):
-  // 0 -> 1 (as many registers as the code wants), 1 -> 4 (128 registers),
-  // 2 -> 3 (168 registers), 3 -> 2
+  // register budget variant (minimum resident blocks of 128 threads per SM)
+  // and row staging: 0 -> 1 (as many registers as the code wants),
+  // 1 -> 4 (128 registers), 2 -> 3 (168 registers), 3 -> 2; 4 -> 3 and
+  // 5 -> 4 with rows staged through shared memory by cp.async
   switch (kp.variant) {
-    case 0: launch_step_minb<1>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 2: launch_step_minb<3>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 3: launch_step_minb<2>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    default: launch_step_minb<4>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 0: launch_step_v<1, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 2: launch_step_v<3, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 3: launch_step_v<2, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 4: launch_step_v<3, true>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    case 5: launch_step_v<4, true>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
+    default: launch_step_v<4, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
   }
   return cudaGetLastError();
 }

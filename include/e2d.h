@@ -251,8 +251,9 @@ int e2d_batch_release(e2d_batch *b, int id);
 int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_instances);
 /* The batch's CUDA stream (a cudaStream_t). */
 int e2d_batch_stream(e2d_batch *b, void **stream);
-/* Tuning: register-budget variant of the batch kernel (0..3: at least 1, 4,
- * 3 or 2 resident blocks of 128 threads per SM) and rows per strip (16..512,
+/* Tuning: variant of the batch kernel (0..3: at least 1, 4, 3 or 2 resident
+ * blocks of 128 threads per SM with rows loaded to registers; 4, 5: 3 or 4
+ * blocks with rows staged through shared memory) and rows per strip (16..512,
  * rounded up to a multiple of 16) for the size classes max(nx, ny) <= 192,
  * <= 512, > 512.  Results do not depend on them.  e2d_batch_autotune times the candidates on the live
  * batch (its iterations advance the instances) and keeps the fastest. */
