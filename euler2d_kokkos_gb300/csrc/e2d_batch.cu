@@ -439,7 +439,7 @@ int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_used) {
 
 int e2d_batch_set_tuning(e2d_batch *b, int variant, const int strip_h[3]) {
   if (!b) return E2D_EINVAL;
-  if (variant >= 0 && variant <= 5) b->variant = variant;
+  if (variant >= 0 && variant < kF32cVariants) b->variant = variant;
   // strip heights are whole CFL fold units (16 rows)
   if (strip_h)
     for (int c = 0; c < 3; ++c)
@@ -499,7 +499,7 @@ int e2d_batch_autotune(e2d_batch *b, int iters_per_trial) {
   // register budget first, then each size class's strip height
   double best_ms = 1e30;
   int best_v = b->variant;
-  for (int v = 0; v < 6 && rc == E2D_OK; ++v) {
+  for (int v = 0; v < kF32cVariants && rc == E2D_OK; ++v) {
     b->variant = v;
     double ms;
     rc = trial(&ms);

@@ -24,6 +24,8 @@
 #include "e2d_common.cuh"
 #include "e2d_internal.h"
 
+#include <type_traits>
+
 namespace e2d {
 namespace {
 
@@ -405,13 +407,12 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
 }
 
 // Shared-memory row ring of the staged march: each warp copies the rows it
-// will need PF_DIST iterations ahead with cp.async (no registers held while
-// the copies fly); a slot holds the 8 planes (hi, lo) x 64 columns of one
-// row, each lane copying and later reading only its own two columns.
-constexpr int PF_DIST = 2;                 // rows copied ahead of their use
-constexpr int RING = PF_DIST + 3;          // rows m-1 .. m+1+PF_DIST
-constexpr int SLOT = 8 * 64;               // floats per slot
-constexpr int RING_FLOATS = WPB * RING * SLOT;
+// will need PFD iterations ahead with cp.async (no registers held while the
+// copies fly) into PFD + 3 slots (rows m-1 .. m+1+PFD); a slot holds the 8
+// planes (hi, lo) x 64 columns of one row, each lane copying and later
+// reading only its own two columns.  PFD = 0: rows loaded to registers.
+constexpr int SLOT = 8 * 64;  // floats per slot
+constexpr size_t ring_bytes(int pfd) { return pfd > 0 ? sizeof(float) * WPB * (pfd + 3) * SLOT : 0; }
 
 __device__ __forceinline__ void cp_async8(float *dst, const float *src) {
   const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
@@ -453,7 +454,7 @@ __device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__re
 // kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
-template <int RS, bool STAGED>
+template <int RS, int PFD>
 __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
@@ -487,14 +488,14 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   // (staged path) the boundary map of the lane's columns and its ring slots
   bool f0 = false, f1 = false;
   int s0 = c0, s1 = c0 + 1;
-  if (STAGED && !direct) {
+  if ((PFD > 0) && !direct) {
     s0 = ghost_source(min(max(c0, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f0);
     s1 = ghost_source(min(max(c0 + 1, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f1);
   }
   float *const lane_ring = ring + 2 * lane;
   // hi of a staged row, ghost flips applied
   auto staged_hi = [&](int r, float2 out[4]) {
-    const float *sl = lane_ring + ((r - rb + 2) % RING) * SLOT;
+    const float *sl = lane_ring + ((r - rb + 2) % (PFD + 3)) * SLOT;
 #pragma unroll
     for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
     if (f0) out[E2D_IU].x = -out[E2D_IU].x;
@@ -503,13 +504,13 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
     if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
   };
-  if (STAGED) {
-    // rows rb-2 .. rb+PF_DIST-1, one commit group each
-    for (int r = rb - 2; r < rb + PF_DIST; ++r) {
-      stage_row(kp, w_in, r, c0, direct, s0, s1, lane_ring + ((r - rb + 2) % RING) * SLOT);
+  if ((PFD > 0)) {
+    // rows rb-2 .. rb+PFD-1, one commit group each
+    for (int r = rb - 2; r < rb + PFD; ++r) {
+      stage_row(kp, w_in, r, c0, direct, s0, s1, lane_ring + ((r - rb + 2) % (PFD + 3)) * SLOT);
       cp_async_commit();
     }
-    cp_async_wait<PF_DIST>();
+    cp_async_wait<(PFD > 0 ? PFD : 0)>();
     float2 u[4];
     staged_hi(rb - 2, u);
     prims2(k, u[0], u[1], u[2], u[3], qa);
@@ -527,12 +528,12 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   // (m-1|m); update of row m-1
   for (int m = rb - 1; m <= re; ++m) {
     float2 qc[4];
-    if (STAGED) {
-      // copy row m+1+PF_DIST (its slot last held row m-2), then wait for row m+1
-      const int rn = m + 1 + PF_DIST;
-      if (rn <= re + 1) stage_row(kp, w_in, rn, c0, direct, s0, s1, lane_ring + ((rn - rb + 2) % RING) * SLOT);
+    if ((PFD > 0)) {
+      // copy row m+1+PFD (its slot last held row m-2), then wait for row m+1
+      const int rn = m + 1 + PFD;
+      if (rn <= re + 1) stage_row(kp, w_in, rn, c0, direct, s0, s1, lane_ring + ((rn - rb + 2) % (PFD + 3)) * SLOT);
       cp_async_commit();
-      cp_async_wait<PF_DIST>();
+      cp_async_wait<(PFD > 0 ? PFD : 0)>();
       float2 u[4];
       staged_hi(m + 1, u);
       prims2(k, u[0], u[1], u[2], u[3], qc);
@@ -546,7 +547,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     const bool upd = (m >= rb + 1) && writer;
     const long long ubase = c0 + (long long)kp.wpitch * (m - 1);
     float2 uhi[4], ulo[4];
-    if (!STAGED && upd) {
+    if (!(PFD > 0) && upd) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         uhi[v] = __ldg(reinterpret_cast<const float2 *>(w_in + ubase + v * kp.wplane));
@@ -626,9 +627,9 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       for (int v = 0; v < 4; ++v) fxl[v] = make_float2(__shfl_up_sync(0xffffffffu, fx_prev[v].y, 1), fx_prev[v].x);
       if (upd) {
         const long long base = ubase;
-        if (STAGED) {
+        if ((PFD > 0)) {
           // row m-1 is interior: its slot holds it unflipped
-          const float *sl = lane_ring + ((m - 1 - rb + 2) % RING) * SLOT;
+          const float *sl = lane_ring + ((m - 1 - rb + 2) % (PFD + 3)) * SLOT;
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
             uhi[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
@@ -690,11 +691,12 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   }
 }
 
-template <int RS, int MINB, bool STAGED>
+extern __shared__ __align__(16) float g_ring[];
+
+template <int RS, int MINB, int PFD>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
                 DevClock *clk, const int use_clock, const double host_dt) {
-  __shared__ __align__(16) float ring[STAGED ? RING_FLOATS : 4];
   const KGeom &g = kp.g;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -731,9 +733,9 @@ __global__ void __launch_bounds__(NT, MINB)
   const int nsy = (g.ny + SH - 1) / SH;
   const int strip = blockIdx.x * WPB + (tid >> 5);
   if (strip < nsx * nsy)
-    march_strip<RS, STAGED>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
-                            use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status,
-                            ring + (STAGED ? (tid >> 5) * RING * SLOT : 0));
+    march_strip<RS, PFD>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
+                         use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status,
+                         g_ring + (tid >> 5) * (PFD + 3) * SLOT);
   if (!use_clock) return;
 
   // the last block to finish advances the loop state (src/main.cpp:139-143)
@@ -786,11 +788,10 @@ __device__ __forceinline__ void batch_finalize(BatchInst &I) {
 // instance's own dt, folds the instance's next CFL maximum, and the last
 // strip of each instance advances that instance's loop state.  Results of an
 // instance do not depend on the other instances in the batch.
-template <int RS, int MINB, bool STAGED>
+template <int RS, int MINB, int PFD>
 __global__ void __launch_bounds__(NT, MINB)
     k_batch_f32c(BatchInst *__restrict__ insts, const int *__restrict__ list_slots,
                  const int *__restrict__ strip_begin, const int n_inst, const int total_strips) {
-  __shared__ __align__(16) float ring[STAGED ? RING_FLOATS : 4];
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * WPB;
   for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < total_strips; w += nwarps) {
@@ -808,9 +809,9 @@ __global__ void __launch_bounds__(NT, MINB)
     const KParams32 &kp = I.kp;
     const int par = I.par;
     const int strip = w - strip_begin[lo];
-    march_strip<RS, STAGED>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
-                            strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
-                            ring + (STAGED ? (threadIdx.x >> 5) * RING * SLOT : 0));
+    march_strip<RS, PFD>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
+                         strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
+                         g_ring + (threadIdx.x >> 5) * (PFD + 3) * SLOT);
     if (lane == 0) {
       __threadfence();
       const unsigned int ticket = atomicAdd(&I.done, 1u);
@@ -842,18 +843,35 @@ int strips_of(const KParams32 &kp) {
   return nsx * ((kp.g.ny + kp.strip_h - 1) / kp.strip_h);
 }
 
-template <int MINB, bool STAGED>
+// Kernel variants: (MINB, PFD) = minimum resident blocks of 128 threads per
+// SM (the register budget) and the row-staging distance (0: registers).
+template <class F>
+static void with_variant(int v, F &&f) {
+  using std::integral_constant;
+  switch (v) {
+    case 0: f(integral_constant<int, 1>{}, integral_constant<int, 0>{}); break;
+    case 2: f(integral_constant<int, 3>{}, integral_constant<int, 0>{}); break;
+    case 3: f(integral_constant<int, 2>{}, integral_constant<int, 0>{}); break;
+    case 4: f(integral_constant<int, 3>{}, integral_constant<int, 2>{}); break;
+    case 5: f(integral_constant<int, 4>{}, integral_constant<int, 2>{}); break;
+    default: f(integral_constant<int, 4>{}, integral_constant<int, 0>{}); break;
+  }
+}
+static_assert(kF32cVariants == 6, "with_variant covers variants 0..5");
+
+template <int MINB, int PFD>
 static void launch_batch_v(int riemann, BatchInst *insts, const int *slots, const int *sb, int n, int total,
                            int grid, cudaStream_t s) {
+  const size_t sm = ring_bytes(PFD);
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_batch_f32c<E2D_RIEMANN_HLLC, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLLC, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
     case E2D_RIEMANN_HLL:
-      k_batch_f32c<E2D_RIEMANN_HLL, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLL, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
     default:
-      k_batch_f32c<E2D_RIEMANN_APPROX, MINB, STAGED><<<grid, NT, 0, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_APPROX, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
   }
 }
@@ -862,15 +880,10 @@ cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const 
                               const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
                               cudaStream_t s) {
   if (n_inst <= 0 || total_strips <= 0) return cudaSuccess;
-  const int *ls = list_slots, *sb = strip_begin;
-  switch (variant) {
-    case 0: launch_batch_v<1, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-    case 2: launch_batch_v<3, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-    case 3: launch_batch_v<2, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-    case 4: launch_batch_v<3, true>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-    case 5: launch_batch_v<4, true>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-    default: launch_batch_v<4, false>(riemann, insts, ls, sb, n_inst, total_strips, grid_blocks, s); break;
-  }
+  with_variant(variant, [&](auto minb, auto pfd) {
+    launch_batch_v<decltype(minb)::value, decltype(pfd)::value>(riemann, insts, list_slots, strip_begin, n_inst,
+                                                                total_strips, grid_blocks, s);
+  });
   return cudaGetLastError();
 }
 
@@ -882,15 +895,11 @@ cudaError_t launch_batch_arm(BatchInst *inst, cudaStream_t s) {
 template <int RS>
 static int batch_occupancy(int variant) {
   int n = 0;
-  cudaError_t e;
-  switch (variant) {
-    case 0: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 1, false>, NT, 0); break;
-    case 2: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3, false>, NT, 0); break;
-    case 3: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 2, false>, NT, 0); break;
-    case 4: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 3, true>, NT, 0); break;
-    case 5: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4, true>, NT, 0); break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, 4, false>, NT, 0); break;
-  }
+  cudaError_t e = cudaErrorInvalidValue;
+  with_variant(variant, [&](auto minb, auto pfd) {
+    constexpr int M = decltype(minb)::value, P = decltype(pfd)::value;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, M, P>, NT, ring_bytes(P));
+  });
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
 
@@ -927,7 +936,30 @@ void make_kparams32(const e2d_params &p, KParams32 *kp) {
   kp->strip_h = default_strip_h(p.nx, p.ny);
 }
 
-cudaError_t configure_f32c_kernels() { return cudaSuccess; }
+// Dynamic plus static shared memory above 48 KB must be enabled per kernel
+// before the first launch (and before any graph capture).
+template <int RS>
+static cudaError_t configure_rs() {
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < kF32cVariants && e == cudaSuccess; ++v)
+    with_variant(v, [&](auto minb, auto pfd) {
+      constexpr int M = decltype(minb)::value, P = decltype(pfd)::value;
+      if (P > 0) {  // the kernels' static shared memory comes on top of the ring
+        e = cudaFuncSetAttribute(k_step_f32c<RS, M, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_bytes(P));
+        if (e == cudaSuccess)
+          e = cudaFuncSetAttribute(k_batch_f32c<RS, M, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)ring_bytes(P));
+      }
+    });
+  return e;
+}
+
+cudaError_t configure_f32c_kernels() {
+  cudaError_t e = configure_rs<E2D_RIEMANN_HLLC>();
+  if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_HLL>();
+  if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_APPROX>();
+  return e;
+}
 
 cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w, cudaStream_t s) {
   dim3 block(64, 4);
@@ -956,18 +988,19 @@ cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, i
   return launch_f32c_dt_to(kp, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status, s);
 }
 
-template <int MINB, bool STAGED>
+template <int MINB, int PFD>
 static void launch_step_v(const KParams32 &kp, int riemann, int blocks, const float *w_in, float *w_out,
                           DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
+  const size_t sm = ring_bytes(PFD);
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_step_f32c<E2D_RIEMANN_HLLC, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLLC, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     case E2D_RIEMANN_HLL:
-      k_step_f32c<E2D_RIEMANN_HLL, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLL, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
     default:
-      k_step_f32c<E2D_RIEMANN_APPROX, MINB, STAGED><<<blocks, NT, 0, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_APPROX, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
       break;
   }
 }
@@ -977,18 +1010,10 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
   const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
   const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
   const int blocks = (nsx * nsy + WPB - 1) / WPB;
-  // register budget variant (minimum resident blocks of 128 threads per SM)
-  // and row staging: 0 -> 1 (as many registers as the code wants),
-  // 1 -> 4 (128 registers), 2 -> 3 (168 registers), 3 -> 2; 4 -> 3 and
-  // 5 -> 4 with rows staged through shared memory by cp.async
-  switch (kp.variant) {
-    case 0: launch_step_v<1, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 2: launch_step_v<3, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 3: launch_step_v<2, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 4: launch_step_v<3, true>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    case 5: launch_step_v<4, true>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-    default: launch_step_v<4, false>(kp, riemann, blocks, w_in, w_out, clk, use_clock, host_dt, s); break;
-  }
+  with_variant(kp.variant, [&](auto minb, auto pfd) {
+    launch_step_v<decltype(minb)::value, decltype(pfd)::value>(kp, riemann, blocks, w_in, w_out, clk, use_clock,
+                                                               host_dt, s);
+  });
   return cudaGetLastError();
 }
 

@@ -125,6 +125,9 @@ void make_kparams32(const e2d_params &p, KParams32 *kp);
 // Ghost cells of these arrays are not maintained: the step reads ghosts
 // through the boundary map.
 cudaError_t configure_f32c_kernels();
+// FP32C step / batch kernel variants (register budget x row staging), see
+// with_variant in e2d_fp32c.cu.
+constexpr int kF32cVariants = 6;
 cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w, cudaStream_t s);
 cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, cudaStream_t s);
 // CFL maximum of a state (interior) into clk->acc[slot] (slot < 0: invdt_bits).
