@@ -414,9 +414,9 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
 constexpr int SLOT = 8 * 64;  // floats per slot
 constexpr size_t ring_bytes(int pfd) { return pfd > 0 ? sizeof(float) * WPB * (pfd + 3) * SLOT : 0; }
 
-__device__ __forceinline__ void cp_async8(float *dst, const float *src) {
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
   const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
   const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
@@ -426,22 +426,35 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Copies array row r (ghost rows through the boundary map) for the lane's two
-// columns into `slot`; `direct`: both columns interior and read as a pair,
-// else columns s0, s1 (the boundary map of c0, c0 + 1).
-__device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__restrict__ w, int r, int c0,
-                                          bool direct, int s0, int s1, float *slot) {
-  const KGeom &g = kp.g;
+// Source row of array row r: itself, or through the boundary map when the
+// strip touches a ghost row (`yghost`, warp-uniform); fv: negate IV.
+__device__ __forceinline__ int source_row(const KGeom &g, int r, bool yghost, bool &fv) {
+  fv = false;
+  if (!yghost) return r;
+  return ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
+}
+
+// Copies array row r into a ring slot.  `direct` strips (64 interior
+// columns starting at array column cs, a multiple of 4) copy 16-byte chunks,
+// lane l taking chunk l % 16 of planes l / 16, +2, +4, +6, so a lane reads
+// columns another lane copied; other strips copy each lane's two columns
+// s0, s1 (the boundary map of c0, c0 + 1) element by element.
+__device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__restrict__ w, int r, int cs,
+                                          int lane, bool direct, bool yghost, int s0, int s1, float *slot) {
   bool fv;
-  const int sr = ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
-  const float *row = w + (long long)sr * kp.wpitch;
+  const float *row = w + (long long)source_row(kp.g, r, yghost, fv) * kp.wpitch;
+  if (direct) {
+    const int chunk = lane & 15;
 #pragma unroll
-  for (int v = 0; v < 8; ++v) {
-    if (direct) {
-      cp_async8(slot + v * 64, row + v * kp.wplane + c0);
-    } else {
-      cp_async4(slot + v * 64, row + v * kp.wplane + s0);
-      cp_async4(slot + v * 64 + 1, row + v * kp.wplane + s1);
+    for (int k = 0; k < 4; ++k) {
+      const int v = (lane >> 4) + 2 * k;
+      cp_async16(slot + v * 64 + 4 * chunk, row + v * kp.wplane + cs + 4 * chunk);
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      cp_async4(slot + v * 64 + 2 * lane, row + v * kp.wplane + s0);
+      cp_async4(slot + v * 64 + 2 * lane + 1, row + v * kp.wplane + s1);
     }
   }
 }
@@ -492,29 +505,36 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     s0 = ghost_source(min(max(c0, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f0);
     s1 = ghost_source(min(max(c0 + 1, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f1);
   }
-  float *const lane_ring = ring + 2 * lane;
+  constexpr int R = PFD + 3;  // ring slots; row r sits in slot (r - rb + 2) mod R
+  const bool yghost = (rb - 2 < 2) || (re + 1 > g.ny + 1);
+  auto slot_of = [&](int sl) { return ring + sl * SLOT; };
+  auto wrap = [](int x) { return x >= R ? x - R : x; };
+  int sm1 = 0;  // slot of row m-1 (the row being updated)
   // hi of a staged row, ghost flips applied
-  auto staged_hi = [&](int r, float2 out[4]) {
-    const float *sl = lane_ring + ((r - rb + 2) % (PFD + 3)) * SLOT;
+  auto staged_hi = [&](int r, int sl, float2 out[4]) {
+    const float *p = slot_of(sl) + 2 * lane;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
+    for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(p + v * 64);
     if (f0) out[E2D_IU].x = -out[E2D_IU].x;
     if (f1) out[E2D_IU].y = -out[E2D_IU].y;
     bool fv;
-    ghost_source(min(max(r, 0), g.jsize - 1), g.ny, g.bc_ymin, g.bc_ymax, fv);
+    source_row(g, r, yghost, fv);
     if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
   };
   if ((PFD > 0)) {
-    // rows rb-2 .. rb+PFD-1, one commit group each
+    // rows rb-2 .. rb+PFD-1 into slots 0 .. PFD+1, one commit group each,
+    // after every lane is done with the ring's previous strip
+    __syncwarp();
     for (int r = rb - 2; r < rb + PFD; ++r) {
-      stage_row(kp, w_in, r, c0, direct, s0, s1, lane_ring + ((r - rb + 2) % (PFD + 3)) * SLOT);
+      stage_row(kp, w_in, r, cb - 2, lane, direct, yghost, s0, s1, slot_of(r - rb + 2));
       cp_async_commit();
     }
     cp_async_wait<(PFD > 0 ? PFD : 0)>();
+    __syncwarp();  // lanes read columns other lanes copied
     float2 u[4];
-    staged_hi(rb - 2, u);
+    staged_hi(rb - 2, 0, u);
     prims2(k, u[0], u[1], u[2], u[3], qa);
-    staged_hi(rb - 1, u);
+    staged_hi(rb - 1, 1, u);
     prims2(k, u[0], u[1], u[2], u[3], qb);
   } else {
     float2 u[4];
@@ -529,13 +549,17 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   for (int m = rb - 1; m <= re; ++m) {
     float2 qc[4];
     if ((PFD > 0)) {
-      // copy row m+1+PFD (its slot last held row m-2), then wait for row m+1
+      // wait for row m+1 (rows m+2 .. m+PFD may still be in flight); the
+      // barrier makes every lane's copies visible to the warp and orders
+      // every lane's reads of row m-2 (previous iteration) before the copy
+      // of row m+1+PFD into that slot
+      cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
+      __syncwarp();
       const int rn = m + 1 + PFD;
-      if (rn <= re + 1) stage_row(kp, w_in, rn, c0, direct, s0, s1, lane_ring + ((rn - rb + 2) % (PFD + 3)) * SLOT);
+      if (rn <= re + 1) stage_row(kp, w_in, rn, cb - 2, lane, direct, yghost, s0, s1, slot_of(wrap(sm1 + R - 1)));
       cp_async_commit();
-      cp_async_wait<(PFD > 0 ? PFD : 0)>();
       float2 u[4];
-      staged_hi(m + 1, u);
+      staged_hi(m + 1, wrap(sm1 + 2), u);
       prims2(k, u[0], u[1], u[2], u[3], qc);
     } else {
       float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
@@ -629,7 +653,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
         const long long base = ubase;
         if ((PFD > 0)) {
           // row m-1 is interior: its slot holds it unflipped
-          const float *sl = lane_ring + ((m - 1 - rb + 2) % (PFD + 3)) * SLOT;
+          const float *sl = slot_of(sm1) + 2 * lane;
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
             uhi[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
@@ -679,6 +703,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       fx_prev[v] = fx[v];
       fy_prev[v] = fy[v];
     }
+    sm1 = wrap(sm1 + 1);
   }
   // the strip's fold-unit winners, one lane each, folded in parallel
   if (target) {
