@@ -88,6 +88,13 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->ph.smallc2 = p.smallc * p.smallc;
   kp->ph.dx = p.dx;
   kp->ph.dy = p.dy;
+  auto inv_pow2 = [](double d) {
+    int e = 0;
+    const double m = std::frexp(d, &e);  // d = m * 2^e, m in [0.5, 1)
+    return (m == 0.5 && 1 - e >= -1022 && 1 - e <= 1023) ? std::ldexp(1.0, 1 - e) : 0.0;
+  };
+  kp->ph.inv_dx_pow2 = inv_pow2(p.dx);
+  kp->ph.inv_dy_pow2 = inv_pow2(p.dy);
 }
 
 namespace {

@@ -336,7 +336,10 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
         const double c = sqrt(ph.gamma0 * p / dd);
         const double vx = c + fabs(ux);
         const double vy = c + fabs(uy);
-        term = vx / ph.dx + vy / ph.dy;
+        // vx / dx + vy / dy, as a product when the divisor is a power of two
+        const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
+        const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
+        term = tx + ty;
         if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) flags |= E2D_FLAG_NONFINITE;
         if (!(rho > 0.0)) flags |= E2D_FLAG_DENSITY;
       }

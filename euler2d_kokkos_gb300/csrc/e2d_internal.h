@@ -48,6 +48,9 @@ struct KPhys {
   R gamma0, gamma6, cfl, slope_type, smallr, smallc, smallp, smallpp;
   R gm1, entho, smallc2;
   R dx, dy;
+  // 1/dx, 1/dy when dx, dy are powers of two (then x / dx == x * (1/dx) bit
+  // for bit: both round the same exact value), else 0
+  R inv_dx_pow2, inv_dy_pow2;
 };
 
 struct KParams64 {
