@@ -364,8 +364,9 @@ def fp64_l1_of(e2d, solve, got):
     path (bit-identical to the reference) run to the same t_end."""
     p64 = solve.params.copy()
     p64.precision = e2d.PRECISION_FP64
-    with e2d.HydroRun(p64.init(), init_problem=False) as h:
-        h.set_state(0, solve.u0)
+    with e2d.HydroRun(p64.init(), init_problem=solve.u0 is None) as h:
+        if solve.u0 is not None:
+            h.set_state(0, solve.u0)
         t, ns = 0.0, 0
         while t < solve.t_end:
             prev = ns

@@ -74,6 +74,7 @@ class _Params(ctypes.Structure):
         ("postshock_pressure", ctypes.c_double), ("postshock_velocity", ctypes.c_double),
         ("shock_loc", ctypes.c_double),
         ("fq_split_x", ctypes.c_double), ("fq_split_y", ctypes.c_double),
+        ("fq_state", (ctypes.c_double * 4) * 4),
         ("implode_shape", ctypes.c_int),
         ("implementationVersion", ctypes.c_int),
         ("precision", ctypes.c_int),
@@ -139,6 +140,7 @@ SIGNATURES = {
 }
 
 _lib = None
+ABI_VERSION = 2  # E2D_ABI_VERSION of include/e2d.h: the layout of _Params
 
 
 def load_library(path: str | None = None, build_if_missing: bool = True) -> ctypes.CDLL:
@@ -157,6 +159,8 @@ def load_library(path: str | None = None, build_if_missing: bool = True) -> ctyp
         fn = getattr(L, name)  # AttributeError if the library lacks a symbol
         fn.argtypes = args
         fn.restype = res
+    if L.e2d_abi_version() != ABI_VERSION:
+        raise OSError(f"{so}: ABI version {L.e2d_abi_version()}, this binding expects {ABI_VERSION}; rebuild it")
     if path is None:
         _lib = L
     return L

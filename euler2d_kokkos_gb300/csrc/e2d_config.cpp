@@ -185,8 +185,12 @@ void params_defaults(e2d_params *p) {
   p->postshock_pressure = (double)1.59e5f;
   p->postshock_velocity = (double)113.5f;
   p->shock_loc = (double)0.170f;
-  p->fq_split_x = (double)0.8f;
-  p->fq_split_y = (double)0.8f;
+  // src/HydroRunFunctors.h:1607-1622: real_t literals, not ini reals
+  p->fq_split_x = 0.8;
+  p->fq_split_y = 0.8;
+  static const double lax_liu_3[4][4] = {
+      {1.5, 1.5, 0.0, 0.0}, {0.5323, 0.3, 1.206, 0.0}, {0.138, 0.029, 1.206, 1.206}, {0.5323, 0.3, 0.0, 1.206}};
+  std::memcpy(p->fq_state, lax_liu_3, sizeof(lax_liu_3));
   p->implode_shape = 0;
   p->implementationVersion = 0;
   p->precision = E2D_PRECISION_FP64;
@@ -275,8 +279,16 @@ int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
   p->blast_nbins = (int)m.get_integer("blast", "nbins", 100);
 
   // extensions of this build (absent keys keep the reference's behaviour)
-  p->fq_split_x = m.get_float("four_quadrant", "split_x", 0.8f);
-  p->fq_split_y = m.get_float("four_quadrant", "split_y", 0.8f);
+  const std::string none = "\x01";
+  auto opt_float = [&](const char *sec, const std::string &key, double dflt) {
+    return m.get_string(sec, key, none) == none ? dflt : (double)m.get_float(sec, key, 0.0f);
+  };
+  p->fq_split_x = opt_float("four_quadrant", "split_x", p->fq_split_x);
+  p->fq_split_y = opt_float("four_quadrant", "split_y", p->fq_split_y);
+  static const char *const fq_names[4] = {"rho_", "p_", "u_", "v_"};
+  for (int q = 0; q < 4; ++q)
+    for (int v = 0; v < 4; ++v)
+      p->fq_state[q][v] = opt_float("four_quadrant", fq_names[v] + std::to_string(q), p->fq_state[q][v]);
   p->implode_shape = (int)m.get_integer("implode", "shape", 0);
   const std::string prec = m.get_string("gb300", "precision", "fp64");
   p->precision = (prec == "fp32c") ? E2D_PRECISION_FP32C : E2D_PRECISION_FP64;

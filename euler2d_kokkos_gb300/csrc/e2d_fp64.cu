@@ -643,13 +643,9 @@ __global__ void k_init_f64(const KParams64 kp, const e2d_params p, double *__res
       if (in && blast_e_inside > 0.0) e = blast_e_inside;
       break;
     }
-    case E2D_PROBLEM_FOUR_QUADRANT: {  // :1578-1665, Lax-Liu case 3
-      const double S[4][4] = {{1.5, 1.5, 0.0, 0.0},
-                              {0.5323, 0.3, 1.206, 0.0},
-                              {0.138, 0.029, 1.206, 1.206},
-                              {0.5323, 0.3, 0.0, 1.206}};
+    case E2D_PROBLEM_FOUR_QUADRANT: {  // :1578-1665 (default states: Lax-Liu case 3)
       const int r = (x < p.fq_split_x) ? ((y < p.fq_split_y) ? 2 : 1) : ((y < p.fq_split_y) ? 3 : 0);
-      const double rho = S[r][0], pr = S[r][1], uu = S[r][2], vv = S[r][3];
+      const double rho = p.fq_state[r][0], pr = p.fq_state[r][1], uu = p.fq_state[r][2], vv = p.fq_state[r][3];
       d = rho;
       mx = uu * rho;
       my = vv * rho;

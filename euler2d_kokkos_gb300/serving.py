@@ -100,8 +100,9 @@ def run_one_at_a_time(solves, chunk=256):
     _sync_device()
     t0 = time.perf_counter()
     for s in solves:
-        with HydroRun(s.params, init_problem=False) as h:
-            h.set_state(0, s.u0)
+        with HydroRun(s.params, init_problem=s.u0 is None) as h:
+            if s.u0 is not None:
+                h.set_state(0, s.u0)
             t, ns = 0.0, 0
             while t < s.t_end:
                 prev = ns

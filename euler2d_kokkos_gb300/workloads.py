@@ -56,35 +56,29 @@ def blast_state(nx, ny, cx, cy, radius, p_in, p_out=0.1, rho=1.0, gamma=1.4):
     return U
 
 
-def shocked_bubble_state(nx, ny, mach, density_ratio, gamma=1.4, shock_x=0.15, bubble=(0.45, 0.5, 0.15)):
-    """Pre-shock gas rho = 1, p = 1 at rest; post-shock state behind a shock
-    of the given Mach number (normal-shock relations); bubble of density
-    density_ratio at the same pressure."""
-    g = gamma
-    r1, p1 = 1.0, 1.0
-    c1 = np.sqrt(g * p1 / r1)
-    M2 = mach * mach
-    r2 = r1 * (g + 1) * M2 / ((g - 1) * M2 + 2)
-    p2 = p1 * (2 * g * M2 - (g - 1)) / (g + 1)
-    us = mach * c1
-    u2 = us * (1 - r1 / r2)
-    X, Y = _centres(nx, ny)
+def shocked_bubble_state(nx, ny, p):
+    """The shocked-bubble state of parameters p (the reference's
+    [shocked_bubble] states: post-shock gas left of shock_loc, a bubble at
+    rest, pre-shock gas at rest elsewhere)."""
+    g = p.gamma0
+    X, Y = _centres(nx, ny, p.xmin, p.ymin, p.xmax, p.ymax)
     U = np.zeros((4, ny + 4, nx + 4))
-    post = X < shock_x
-    inb = (X - bubble[0]) ** 2 + (Y - bubble[1]) ** 2 < bubble[2] ** 2
-    rho = np.where(post, r2, np.where(inb, density_ratio * r1, r1))
-    p = np.where(post, p2, p1)
-    u = np.where(post, u2, 0.0)
+    post = X < p.shock_loc
+    inb = np.sqrt((X - p.bubble_center_x) ** 2 + (Y - p.bubble_center_y) ** 2) < p.bubble_radius
+    rho = np.where(post, p.postshock_density, np.where(inb, p.bubble_density, p.preshock_density))
+    pr = np.where(post, p.postshock_pressure, np.where(inb, p.bubble_pressure, p.preshock_pressure))
+    u = np.where(post, p.postshock_velocity, 0.0)
     U[0] = rho
     U[2] = rho * u
-    U[1] = p / (g - 1) + 0.5 * rho * u * u
+    U[1] = pr / (g - 1) + 0.5 * rho * u * u
     return U
 
 
 class Solve:
-    """One request: parameters, initial state, t_end."""
+    """One request: parameters, initial state, t_end.  u0 None: the initial
+    condition is described by the parameters and built on the device."""
 
-    def __init__(self, kind, params: HydroParams, u0: np.ndarray, t_end: float):
+    def __init__(self, kind, params: HydroParams, u0, t_end: float):
         self.kind = kind
         self.params = params
         self.u0 = u0
@@ -94,16 +88,47 @@ class Solve:
     def cells(self):
         return self.params.nx * self.params.ny
 
+    def host_state(self) -> np.ndarray:
+        """The initial state on the host (the generator's own arrays)."""
+        return self.u0 if self.u0 is not None else _host_state(self)
+
+
+def _host_state(s: "Solve") -> np.ndarray:
+    p = s.params
+    if s.kind == "blast":
+        return blast_state(p.nx, p.ny, p.blast_center_x, p.blast_center_y, p.blast_radius,
+                           p.blast_pressure_in, p.blast_pressure_out, rho=p.blast_density_in, gamma=p.gamma0)
+    if s.kind == "four_quadrant":
+        prim = [tuple(p.fq_state[q][v] for v in range(4)) for q in range(4)]
+        return four_quadrant_state(p.nx, p.ny, prim, gamma=p.gamma0, split=(p.fq_split_x, p.fq_split_y))
+    if s.kind == "shocked_bubble":
+        return shocked_bubble_state(p.nx, p.ny, p)
+    raise ValueError("no host generator for " + s.kind)
+
 
 def _side(rng, lo=64, hi=1024):
     s = np.exp(rng.uniform(np.log(lo), np.log(hi)))
     return int(min(hi, max(lo, 16 * round(s / 16))))
 
 
+def shock_states(mach, gamma=1.4):
+    """Post-shock (rho, p, u) behind a normal shock of the given Mach number
+    running into gas at rest with rho = 1, p = 1 (Rankine-Hugoniot)."""
+    g = gamma
+    M2 = mach * mach
+    r2 = (g + 1) * M2 / ((g - 1) * M2 + 2)
+    p2 = (2 * g * M2 - (g - 1)) / (g + 1)
+    u2 = mach * np.sqrt(g) * (1 - 1 / r2)
+    return r2, p2, u2
+
+
 def mixed_batch(n: int, seed: int = 0, *, max_side: int = 1024, bubbles: bool = False,
-                precision: int = PRECISION_FP32C, riemann: str = "hllc"):
+                precision: int = PRECISION_FP32C, riemann: str = "hllc", device_init: bool = True):
     """n solves: blasts and four-quadrant problems (and shocked bubbles when
-    `bubbles`), in a seeded order."""
+    `bubbles`), in a seeded order.  Each initial condition is carried by its
+    parameters (the reference's [blast] and [shocked_bubble] states, the
+    four-quadrant states and split) and built on the device at admission;
+    device_init=False attaches the host-generated arrays instead."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n):
@@ -117,23 +142,34 @@ def mixed_batch(n: int, seed: int = 0, *, max_side: int = 1024, bubbles: bool = 
             ratio = np.exp(rng.uniform(np.log(10.0), np.log(1e4)))
             p = make_params(nx, ny, problem="blast", riemann=riemann, gamma0=1.4, cfl=0.8,
                             bc=(1, 1, 1, 1), precision=precision)
-            u0 = blast_state(nx, ny, cx, cy, radius, 0.1 * ratio, gamma=p.gamma0)
+            p.blast_center_x, p.blast_center_y, p.blast_radius = float(cx), float(cy), float(radius)
+            p.blast_density_in = p.blast_density_out = 1.0
+            p.blast_pressure_in, p.blast_pressure_out = 0.1 * float(ratio), 0.1
+            p.blast_total_energy_inside = 0.0
         elif kind == "four_quadrant":
-            prim = []
-            for _ in range(4):
+            p = make_params(nx, ny, problem="four_quadrant", riemann=riemann, gamma0=1.4, cfl=0.8,
+                            bc=(2, 2, 2, 2), precision=precision)
+            p.fq_split_x = p.fq_split_y = 0.5
+            for q in range(4):
                 rho = rng.uniform(0.1, 2.0)
                 pr = rng.uniform(0.02, 2.0)
                 u = rng.uniform(0.0, 1.5) * rng.choice([-1.0, 1.0])
                 v = rng.uniform(0.0, 1.5) * rng.choice([-1.0, 1.0])
-                prim.append((rho, pr, u, v))
-            p = make_params(nx, ny, problem="four_quadrant", riemann=riemann, gamma0=1.4, cfl=0.8,
-                            bc=(2, 2, 2, 2), precision=precision)
-            u0 = four_quadrant_state(nx, ny, prim, gamma=p.gamma0)
+                for i, val in enumerate((rho, pr, u, v)):
+                    p.fq_state[q][i] = float(val)
         else:
             mach = rng.uniform(1.2, 3.0)
             ratio = rng.uniform(0.1, 10.0)
             p = make_params(nx, ny, problem="shocked_bubble", riemann=riemann, gamma0=1.4, cfl=0.8,
                             bc=(2, 2, 1, 1), precision=precision)
-            u0 = shocked_bubble_state(nx, ny, mach, ratio, gamma=p.gamma0)
-        out.append(Solve(kind, p, u0, t_end))
+            r2, p2, u2 = shock_states(float(mach), p.gamma0)
+            p.shock_loc = 0.15
+            p.bubble_center_x, p.bubble_center_y, p.bubble_radius = 0.45, 0.5, 0.15
+            p.bubble_density, p.bubble_pressure = float(ratio), 1.0
+            p.preshock_density, p.preshock_pressure = 1.0, 1.0
+            p.postshock_density, p.postshock_pressure, p.postshock_velocity = r2, p2, u2
+        s = Solve(kind, p, None, t_end)
+        if not device_init:
+            s.u0 = _host_state(s)
+        out.append(s)
     return out

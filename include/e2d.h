@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define E2D_ABI_VERSION 1
+#define E2D_ABI_VERSION 2
 
 typedef enum e2d_status {
   E2D_OK = 0,
@@ -88,8 +88,13 @@ typedef struct e2d_params {
   double bubble_radius, bubble_center_x, bubble_center_y, bubble_density, bubble_pressure;
   double preshock_density, preshock_pressure, postshock_density, postshock_pressure;
   double postshock_velocity, shock_loc;
-  /* [four_quadrant] split point (the reference hard-codes 0.8, 0.8) */
+  /* [four_quadrant] split point (the reference hard-codes 0.8, 0.8) and the
+   * primitive state (rho, p, u, v) of quadrants 0 (x >= split_x, y >=
+   * split_y), 1 (x < split_x, y >= split_y), 2 (both below), 3 (x >=
+   * split_x, y < split_y); defaults: the reference's Lax-Liu case 3
+   * (src/HydroRunFunctors.h:1607-1622), ini keys rho_q, p_q, u_q, v_q */
   double fq_split_x, fq_split_y;
+  double fq_state[4][4];
   /* [implode] shape: 0 = the reference's x + y*y in (0.5, 1.5) band,
    * 1 = the classic diagonal split x + y > 0.5 */
   int implode_shape;

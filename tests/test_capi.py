@@ -32,7 +32,7 @@ def test_library_exports_every_declared_symbol():
 
 def test_abi_version_and_status_strings():
     L = e2d.load_library()
-    assert L.e2d_abi_version() == 1
+    assert L.e2d_abi_version() == e2d.ABI_VERSION == 2
     for s in range(7):
         assert L.e2d_status_string(s)
 
@@ -67,6 +67,22 @@ def test_params_blast_and_bubble_values(tmp_path):
     assert p.blast_density_out == C.f32(1.2)  # reference default
     assert p.blast_center_x == C.f32(0.5)     # (xmin+xmax)/2
     assert p.shock_loc == C.f32(0.3)
+
+
+def test_params_four_quadrant_states(tmp_path):
+    """Defaults: the reference's hard-coded Lax-Liu case 3 and split 0.8 as
+    FP64 literals (src/HydroRunFunctors.h:1607-1622); keys rho_q, p_q, u_q,
+    v_q and split_x/y override them through the ini's float rounding."""
+    p = e2d.HydroParams.from_ini(C.write_ini(C.ini_text(16, 16, problem="four_quadrant"), str(tmp_path)))
+    assert (p.fq_split_x, p.fq_split_y) == (0.8, 0.8)
+    assert [list(r) for r in p.fq_state] == [[1.5, 1.5, 0.0, 0.0], [0.5323, 0.3, 1.206, 0.0],
+                                             [0.138, 0.029, 1.206, 1.206], [0.5323, 0.3, 0.0, 1.206]]
+    text = C.ini_text(16, 16, problem="four_quadrant",
+                      extra="[four_quadrant]\nsplit_x=0.5\nrho_2=0.7\nv_3=-0.25\n")
+    p = e2d.HydroParams.from_ini(C.write_ini(text, str(tmp_path), "b.ini"))
+    assert p.fq_split_x == 0.5 and p.fq_split_y == 0.8
+    assert p.fq_state[2][0] == C.f32(0.7) and p.fq_state[3][3] == -0.25
+    assert p.fq_state[0][0] == 1.5
 
 
 def test_params_validation():
