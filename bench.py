@@ -239,8 +239,8 @@ def run_reference_arm(args, rank):
 
 
 def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
-            with_e2e=True, with_clocks=True):
-    p = workload_params(e2d, problem, nx, args.riemann, precision)
+            with_e2e=True, with_clocks=True, riemann=None):
+    p = workload_params(e2d, problem, nx, riemann or args.riemann, precision)
     h = e2d.HydroRun(p)
     stream = torch.cuda.ExternalStream(h.stream())
     t_end = 10.0
@@ -526,6 +526,13 @@ def main():
             "ms_per_step": s["ms"] / args.steps,
             "roofline": roofline(s["kernels"], "fp32c", sc, "k_step_f32c"),
             "accuracy": l1_check(e2d, 1024, 0.3)}
+        # C2 also names the HLL solver: the same FP64 blast with it
+        hl = measure(e2d, torch, args, "fp64", args.problem, nx, args.steps, args.warmup, local,
+                     barrier, None, with_e2e=False, with_clocks=False, riemann="hll")
+        line["hll"] = {"config": config(args.problem, nx, "hll", "fp64"),
+                       "value": cells * args.steps / (hl["ms"] / 1e3) / 1e9, "unit": METRIC,
+                       "ms_per_step": hl["ms"] / args.steps,
+                       "roofline": roofline(hl["kernels"], "fp64", cells, "k_flux_update")}
         # batched mixed solves against one at a time, and one loaded serving point
         line["batch"] = batch_summary(512, 24)
         line["serve"] = {"workload": SERVE_WORKLOAD, "sweep": serve_summary([32.0], 10.0, 320)}

@@ -129,15 +129,12 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
   const float2 etotstar = fma2(ptotstar, ustar, fma2(sdu, es, neg2(ps * us))) * isds;
   // SL > 0: left state; else star (left or right); SR <= 0: right state.
   // Supersonic faces are rare: a warp with none of them skips the selects.
-  float2 ro = rstar, uo = ustar, po = ptotstar, eo = etotstar;
   const bool sx = SL.x > 0.0f, sy = SL.y > 0.0f;
   const bool tx = !sx && (lx || SR.x > 0.0f), ty = !sy && (ly || SR.y > 0.0f);
-  if (__any_sync(0xffffffffu, !(tx && ty))) {
-    ro = sel2(sx, sy, rl, sel2(tx, ty, rstar, rr));
-    uo = sel2(sx, sy, ul, sel2(tx, ty, ustar, ur));
-    po = sel2(sx, sy, pl, sel2(tx, ty, ptotstar, pr));
-    eo = sel2(sx, sy, etotl, sel2(tx, ty, etotstar, etotr));
-  }
+  const float2 ro = sel2(sx, sy, rl, sel2(tx, ty, rstar, rr));
+  const float2 uo = sel2(sx, sy, ul, sel2(tx, ty, ustar, ur));
+  const float2 po = sel2(sx, sy, pl, sel2(tx, ty, ptotstar, pr));
+  const float2 eo = sel2(sx, sy, etotl, sel2(tx, ty, etotstar, etotr));
   f[E2D_ID] = ro * uo;
   f[E2D_IU] = fma2(f[E2D_ID], uo, po);
   f[E2D_IP] = (eo + po) * uo;
@@ -603,46 +600,43 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       s0[E2D_IU] = neg2(fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir)));
       s0[E2D_IV] = neg2(fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir)));
     }
-    // x faces of row m and their fluxes (needed for rows rb..re-1)
-    float2 fx[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
-    if (m >= rb && m < re) {
-      float2 xl[4], xr[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const float2 h = k.half * dqx[v];
-        const float2 s = k.half * s0[v] * dtdx;
-        float2 xmin = (qb[v] - h) + s;
-        float2 xmax = (qb[v] + h) + s;
-        if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
-        xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
-        xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
-      }
-      riemann2<RS>(ph, k, xl, xr, fx);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
-    }
-    // y faces of row m; flux of face (m-1|m) from the saved YMAX of row m-1
-    float2 ymin[4], ymax[4];
+    // x faces of row m (fluxes needed for rows rb..re-1) and y faces of row
+    // m (the flux of face (m-1|m) from the saved YMAX of row m-1, needed for
+    // m >= rb).  Both Riemann solves run on every row, their results masked
+    // outside those rows: the loop body has no branch around them, so the
+    // two independent solves can be scheduled together.
+    float2 xl[4], xr[4], ymin[4], ymax[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const float2 h = k.half * dqy[v];
-      const float2 s = k.half * s0[v] * dtdy;
-      ymin[v] = (qb[v] - h) + s;
-      ymax[v] = (qb[v] + h) + s;
+      const float2 hx = k.half * dqx[v];
+      const float2 sx_ = k.half * s0[v] * dtdx;
+      float2 xmin = (qb[v] - hx) + sx_;
+      float2 xmax = (qb[v] + hx) + sx_;
+      if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
+      xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
+      xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
+      const float2 hy = k.half * dqy[v];
+      const float2 sy_ = k.half * s0[v] * dtdy;
+      ymin[v] = (qb[v] - hy) + sy_;
+      ymax[v] = (qb[v] + hy) + sy_;
     }
     ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
     ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
-    float2 fy[4] = {f2(0.0f), f2(0.0f), f2(0.0f), f2(0.0f)};
-    if (m >= rb) {
+    float2 fx[4], fy[4];
+    {
       // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
       float2 yl[4] = {ymax_prev[E2D_ID], ymax_prev[E2D_IP], ymax_prev[E2D_IV], ymax_prev[E2D_IU]};
       float2 yr[4] = {ymin[E2D_ID], ymin[E2D_IP], ymin[E2D_IV], ymin[E2D_IU]};
       float2 f[4];
+      riemann2<RS>(ph, k, xl, xr, fx);
       riemann2<RS>(ph, k, yl, yr, f);
-      fy[E2D_ID] = f[E2D_ID] * dtdy;
-      fy[E2D_IP] = f[E2D_IP] * dtdy;
-      fy[E2D_IU] = f[E2D_IV] * dtdy;
-      fy[E2D_IV] = f[E2D_IU] * dtdy;
+      const bool xrow = (m >= rb) && (m < re), yrow = m >= rb;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) fx[v] = xrow ? fx[v] * dtdx : f2(0.0f);
+      fy[E2D_ID] = yrow ? f[E2D_ID] * dtdy : f2(0.0f);
+      fy[E2D_IP] = yrow ? f[E2D_IP] * dtdy : f2(0.0f);
+      fy[E2D_IU] = yrow ? f[E2D_IV] * dtdy : f2(0.0f);
+      fy[E2D_IV] = yrow ? f[E2D_IU] * dtdy : f2(0.0f);
     }
     // compensated update of row m-1
     if (m >= rb + 1) {
