@@ -244,6 +244,19 @@ def run_reference_arm(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(dist, x: float) -> float:
+    """The largest x over all ranks (the job's time is its slowest rank's);
+    x itself without a process group."""
+    if not dist:
+        return x
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
             with_e2e=True, with_clocks=True, riemann=None):
     p = workload_params(e2d, problem, nx, riemann or args.riemann, precision)
@@ -278,12 +291,7 @@ def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barr
     t, ns, _ = h.step_n(steps, t_end, t, ns)
     ev1.record(stream)
     barrier()
-    ms = ev0.elapsed_time(ev1)
-    ms_max = ms
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_max = float(tt.item())
+    ms_max = max_over_ranks(dist, ev0.elapsed_time(ev1))
     out = {"ms": ms_max, "ms_profiled": ms_prof, "kernels": kt,
            "clocks": sampler.summary() if sampler else None}
     if with_e2e:
@@ -299,8 +307,9 @@ def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barr
         h.set_state(0, host_in)
         _, ns2, _ = h.step_n(steps, t_end, 0.0, 0)
         h.get_state(ns2 % 2, host_out)
-        e2e_s = time.perf_counter() - t0
-        out["e2e"] = {"value": nx * nx * ns2 / e2e_s / 1e9, "unit": METRIC,
+        e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        world = dist.get_world_size() if dist else 1
+        out["e2e"] = {"value": nx * nx * ns2 * world / e2e_s / 1e9, "unit": METRIC,
                       "h2d_bytes_per_step": host_in.nbytes / max(ns2, 1),
                       "d2h_bytes_per_step": (host_out.nbytes + 8 * ns2) / max(ns2, 1),
                       "path": "e2d_set_state + e2d_step_n + e2d_get_state from pinned host buffers, "
