@@ -95,6 +95,8 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   };
   kp->ph.inv_dx_pow2 = inv_pow2(p.dx);
   kp->ph.inv_dy_pow2 = inv_pow2(p.dy);
+  kp->tile = 0;
+  if (const char *v = std::getenv("E2D_F64_TILE")) kp->tile = std::atoi(v);
 }
 
 namespace {

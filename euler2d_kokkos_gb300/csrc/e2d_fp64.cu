@@ -8,7 +8,7 @@
 //                      (ConvertToPrimitivesFunctor, src/HydroRunFunctors.h:84-143)
 //                      and the CFL maximum of the interior
 //                      (ComputeDtFunctor, src/HydroRunFunctors.h:17-79);
-//   k_flux_update_f64  per 32x16 tile: limited slopes once per cell, the
+//   k_flux_update_f64  per 32x32 tile: limited slopes once per cell, the
 //                      half-step trace once per cell and face, one Riemann
 //                      solve per face, the conservative update
 //                      (ComputeAndStoreFluxesFunctor + UpdateFunctor,
@@ -32,16 +32,15 @@ using f64x::max_pos;
 using f64x::max_any;
 using f64x::min_any;
 
-constexpr int TX = 32;        // interior cells per tile along x
-constexpr int TY = 16;        // interior cells per tile along y
-constexpr int QW = TX + 4;    // primitives tile width (2-cell halo)
-constexpr int QH = TY + 4;
-constexpr int XW = TX + 2;    // x-face states: cells x in [-1, TX]
-constexpr int YH = TY + 2;    // y-face states: cells y in [-1, TY]
-constexpr int NT = 256;       // threads per tile block
 constexpr int FILL_BX = 64, FILL_BY = 4;
 
-constexpr size_t kSmemDoubles = 4 * QH * QW + 2 * (4 * TY * XW) + 2 * (4 * YH * TX);
+// Shared memory of a TX x TY tile of the flux kernel: primitives with a
+// 2-cell halo, then XMIN/XMAX states of cells x in [-1, TX] and YMIN/YMAX
+// states of cells y in [-1, TY].
+template <int TX, int TY>
+constexpr size_t flux_smem_bytes() {
+  return sizeof(double) * (4 * (TY + 4) * (TX + 4) + 2 * (4 * TY * (TX + 2)) + 2 * (4 * (TY + 2) * TX));
+}
 
 __device__ __forceinline__ int src_lo_hi(int i, int n, int bc_lo, int bc_hi, bool &flip) {
   return ghost_source(i, n, bc_lo, bc_hi, flip);
@@ -372,11 +371,21 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
 }
 
 // ------------------------------------------------------------ kernel 2
-template <int RS>
-__global__ void __launch_bounds__(NT, 2)
+// Tile shapes (kp.tile): 0 -> 32 x 32 cells, 512 threads, 1 block per SM
+// (180.7 KB shared; 1.125 slope/trace evaluations and 2.06 Riemann solves
+// per cell); 1 -> 32 x 16, 256 threads, 2 blocks per SM (94.7 KB; 1.19 and
+// 2.09).  Measured on the 4096^2 blast: 15.12 and 15.38 ms per step; smaller
+// tiles (16 x 16, 32 x 8: 16.1, 16.7 ms) lose more to halo work than they
+// gain in residency.  Results do not depend on the shape.
+template <int RS, int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     k_flux_update_f64(const KParams64 kp, const double *__restrict__ q,
                       const double *__restrict__ u_in, double *__restrict__ u_out, DevClock *clk,
                       const int use_clock, const double host_dt, double *__restrict__ dt_trace) {
+  constexpr int QW = TX + 4;  // primitives tile width (2-cell halo)
+  constexpr int QH = TY + 4;
+  constexpr int XW = TX + 2;  // x-face states: cells x in [-1, TX]
+  constexpr int YH = TY + 2;  // y-face states: cells y in [-1, TY]
   extern __shared__ double smem[];
   double *sQ = smem;                   // [4][QH][QW]  primitives with halo
   double *sXm = sQ + 4 * QH * QW;      // [4][TY][XW]  XMIN states, then x-fluxes
@@ -688,7 +697,6 @@ __global__ void k_init_f64(const KParams64 kp, const e2d_params p, double *__res
 
 }  // namespace
 
-size_t flux_update_f64_smem_bytes() { return kSmemDoubles * sizeof(double); }
 
 cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, double *q,
                             DevClock *clk, int mode, cudaStream_t s) {
@@ -698,24 +706,43 @@ cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, do
   return cudaGetLastError();
 }
 
+template <int RS, int TX, int TY, int NT, int MINB>
+static cudaError_t launch_flux_shape(const KParams64 &kp, const double *q, const double *u_in,
+                                     double *u_out, DevClock *clk, int use_clock, double host_dt,
+                                     double *dt_trace, cudaStream_t s) {
+  dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
+  k_flux_update_f64<RS, TX, TY, NT, MINB><<<grid, NT, flux_smem_bytes<TX, TY>(), s>>>(
+      kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace);
+  return cudaGetLastError();
+}
+
 template <int RS>
 static cudaError_t launch_flux_t(const KParams64 &kp, const double *q, const double *u_in,
                                  double *u_out, DevClock *clk, int use_clock, double host_dt,
                                  double *dt_trace, cudaStream_t s) {
-  dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
-  k_flux_update_f64<RS><<<grid, NT, flux_update_f64_smem_bytes(), s>>>(kp, q, u_in, u_out, clk,
-                                                                      use_clock, host_dt, dt_trace);
-  return cudaGetLastError();
+  if (kp.tile == 1)
+    return launch_flux_shape<RS, 32, 16, 256, 2>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
+  return launch_flux_shape<RS, 32, 32, 512, 1>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
+}
+
+template <int RS, int TX, int TY, int NT, int MINB>
+static cudaError_t set_flux_smem() {
+  return cudaFuncSetAttribute(k_flux_update_f64<RS, TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)flux_smem_bytes<TX, TY>());
+}
+
+template <int RS>
+static cudaError_t configure_rs() {
+  cudaError_t e = set_flux_smem<RS, 32, 32, 512, 1>();
+  if (e == cudaSuccess) e = set_flux_smem<RS, 32, 16, 256, 2>();
+  return e;
 }
 
 cudaError_t configure_f64_kernels() {
-  const int smem = (int)flux_update_f64_smem_bytes();
-  cudaError_t e;
-  e = cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_HLLC>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_HLL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_flux_update_f64<E2D_RIEMANN_APPROX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  cudaError_t e = configure_rs<E2D_RIEMANN_HLLC>();
+  if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_HLL>();
+  if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_APPROX>();
+  return e;
 }
 
 cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const double *q,

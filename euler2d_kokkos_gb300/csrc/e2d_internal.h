@@ -56,6 +56,7 @@ struct KPhys {
 struct KParams64 {
   KGeom g;
   KPhys<double> ph;
+  int tile;  // flux kernel tile shape (see k_flux_update_f64)
 };
 
 // FP32 step with FP64 copies of the constants the exact dt recompute uses.
@@ -177,7 +178,6 @@ size_t reduce_partial_count(const KGeom &g);
 cudaError_t launch_sums_f64(const KGeom &g, const double *u, double *partial, double *out4, cudaStream_t s);
 cudaError_t launch_l1diff_f64(const KGeom &g, const double *a, const double *b, int var,
                               double *partial, double *out2, cudaStream_t s);
-size_t flux_update_f64_smem_bytes();
 
 // Radial density profile about the box centre (e2d_reduce.cu), over every
 // cell of the array including ghosts; rings >= nbins are not counted.
