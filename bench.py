@@ -399,22 +399,28 @@ SERVE_WORKLOAD = ("Poisson arrivals of blasts, four-quadrant problems and shocke
                   "density ratio 0.1..10), grids 64^2..2048^2, t_end U[0.05,0.25], 150 GB pool, HLLC, CFL 0.8")
 
 
-def batch_summary(instances, sample):
+def batch_summary(instances, sample, fp64=False):
     """Mixed 64^2-1024^2 blasts and four-quadrant problems (seed 0), each to
     its own t_end: one batched run of all of them against the same kind of
-    solves run one at a time, FP32 compensated, HLLC, CFL 0.8."""
+    solves run one at a time, HLLC, CFL 0.8; FP32 compensated (with the L1
+    error of the smallest sampled solves against the FP64 path), or FP64
+    (each result bit-identical to the single FP64 path)."""
     import euler2d_kokkos_gb300 as e2d
     from euler2d_kokkos_gb300 import serving, workloads
 
-    solves = workloads.mixed_batch(instances, seed=0)
+    prec = e2d.PRECISION_FP64 if fp64 else e2d.PRECISION_FP32C
+    solves = workloads.mixed_batch(instances, seed=0, precision=prec)
     stride = max(1, len(solves) // sample)
     sample_idx = list(range(0, len(solves), stride))[:sample]
     # accuracy: the smallest sampled solves against the FP64 path
-    small = sorted(sample_idx, key=lambda k: solves[k].cells)[:3]
+    small = [] if fp64 else sorted(sample_idx, key=lambda k: solves[k].cells)[:3]
     bstats, states = serving.run_batched(solves, pool_bytes=64 << 30, keep=set(small))
     seq = serving.run_one_at_a_time([solves[k] for k in sample_idx])
     l1 = [fp64_l1_of(e2d, solves[k], states[k]) for k in small if k in states]
+    out_l1 = {"bitwise_equal_to_single_fp64_path": "tests/test_gpu_batch.py"} if fp64 else \
+        {"rel_l1_density_vs_fp64": l1}
     return {"workload": f"{len(solves)} {BATCH_WORKLOAD}", "instances": len(solves),
+            "precision": "fp64" if fp64 else "fp32c",
             "cells_total": sum(s.cells for s in solves),
             "tuning": {"variant": bstats.tuning[0], "strip_h_per_class": bstats.tuning[1]},
             "value": bstats.gcell_per_s, "unit": METRIC,
@@ -424,7 +430,7 @@ def batch_summary(instances, sample):
                               "cell_updates": seq.cell_updates,
                               "sample": f"{len(sample_idx)} of the {len(solves)} solves, every {stride}th"},
             "batched_over_one_at_a_time": bstats.gcell_per_s / seq.gcell_per_s if seq.gcell_per_s else None,
-            "rel_l1_density_vs_fp64": l1}
+            **out_l1}
 
 
 def serve_summary(rates, seconds, max_requests):
@@ -455,10 +461,11 @@ def mode_line(value, mode, config_, extra):
 def batch_mode(args):
     with ClockSampler(0) as clocks:
         b = batch_summary(args.instances, args.sample)
+        b64 = batch_summary(max(8, args.instances // 8), max(2, args.sample // 3), fp64=True)
     line = mode_line(b["value"], "batch", {"workload": b["workload"], "instances": b["instances"],
                                            "cells_total": b["cells_total"], "tuning": b["tuning"]},
-                     {k: b[k] for k in ("batched", "one_at_a_time", "batched_over_one_at_a_time",
-                                        "rel_l1_density_vs_fp64")})
+                     {**{k: b[k] for k in ("batched", "one_at_a_time", "batched_over_one_at_a_time",
+                                           "rel_l1_density_vs_fp64")}, "fp64": b64})
     line["steps"] = b["batched"]["launch_iterations"]
     line["ms_per_step"] = b["batched"]["seconds"] * 1e3 / max(line["steps"], 1)
     line["clocks"] = clocks.summary()
@@ -550,6 +557,7 @@ def main():
                        "roofline": roofline(hl["kernels"], "fp64", cells, "k_flux_update")}
         # batched mixed solves against one at a time, and one loaded serving point
         line["batch"] = batch_summary(512, 24)
+        line["batch_fp64"] = batch_summary(64, 8, fp64=True)
         line["serve"] = {"workload": SERVE_WORKLOAD, "sweep": serve_summary([32.0], 10.0, 320)}
 
     if rank == 0 and not args.no_cpu_baseline:

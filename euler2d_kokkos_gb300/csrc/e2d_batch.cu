@@ -73,10 +73,16 @@ class PoolAllocator {
 
 struct HostInst {
   bool used = false;
+  bool fp64 = false;  // an FP64 instance (BatchInst64 table), else FP32C
   e2d_params p{};
   size_t off = 0, bytes = 0;
   int size_class = 0;
-  BatchInst mirror{};  // last downloaded copy of the device entry
+  BatchInst mirror{};      // last downloaded copy of the device entry (FP32C)
+  BatchInst64 mirror64{};  // (FP64)
+  double t() const { return fp64 ? mirror64.t : mirror.t; }
+  int nstep() const { return fp64 ? mirror64.nstep : mirror.nstep; }
+  int active() const { return fp64 ? mirror64.active : mirror.active; }
+  unsigned int status() const { return fp64 ? mirror64.status : mirror.status; }
 };
 
 int size_class_of(int nx, int ny) {
@@ -100,6 +106,10 @@ struct e2d_batch {
   int *d_list = nullptr;         // [0, max_inst): slot of list entry k; then strip_begin (max_inst + 1)
   std::vector<int> list;         // slots of the current work list
   int total_strips = 0;
+  BatchInst64 *d_insts64 = nullptr;  // slot-indexed FP64 table
+  int *d_list64 = nullptr;           // slots, then fill_begin, then tile_begin (max_inst + 1 each)
+  std::vector<int> list64;           // slots of the current FP64 work list
+  int total_fill = 0, total_tiles = 0;
   bool list_dirty = true;
   int grid = 0;
   std::map<int, cudaGraphExec_t> graphs;  // iterations -> graph of the current list
@@ -128,14 +138,56 @@ void drop_graphs(e2d_batch *b) {
 }
 
 size_t inst_bytes(const KParams32 &kp) { return (size_t)2 * 8 * kp.wplane * sizeof(float); }
+// FP64 instance: U, U2 and the primitive array
+size_t inst_bytes64(const KGeom &g) { return (size_t)3 * 4 * g.plane * sizeof(double); }
 
 int sync_mirrors(e2d_batch *b) {
   std::vector<BatchInst> tmp(b->max_inst);
+  std::vector<BatchInst64> tmp64(b->max_inst);
   B_CK(b, cudaMemcpyAsync(tmp.data(), b->d_insts, sizeof(BatchInst) * b->max_inst, cudaMemcpyDeviceToHost,
                           b->stream), "table download");
+  B_CK(b, cudaMemcpyAsync(tmp64.data(), b->d_insts64, sizeof(BatchInst64) * b->max_inst, cudaMemcpyDeviceToHost,
+                          b->stream), "table download");
   B_CK(b, cudaStreamSynchronize(b->stream), "table sync");
-  for (int k = 0; k < b->max_inst; ++k)
-    if (b->slots[k].used) b->slots[k].mirror = tmp[k];
+  for (int k = 0; k < b->max_inst; ++k) {
+    HostInst &h = b->slots[k];
+    if (!h.used) continue;
+    if (h.fp64)
+      h.mirror64 = tmp64[k];
+    else
+      h.mirror = tmp[k];
+  }
+  return E2D_OK;
+}
+
+// The FP64 work list: used, active FP64 instances with their fill blocks
+// and flux tiles.
+int rebuild_list64(e2d_batch *b) {
+  std::vector<int> list, fb, tb;
+  int nf = 0, nt = 0;
+  for (int k = 0; k < b->max_inst; ++k) {
+    HostInst &h = b->slots[k];
+    if (!h.used || !h.fp64 || !h.mirror64.active) continue;
+    list.push_back(k);
+    fb.push_back(nf);
+    tb.push_back(nt);
+    nf += h.mirror64.nfill;
+    nt += h.mirror64.ntiles;
+  }
+  fb.push_back(nf);
+  tb.push_back(nt);
+  if (!list.empty()) {
+    const size_t m = (size_t)b->max_inst;
+    B_CK(b, cudaMemcpyAsync(b->d_list64, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, b->stream),
+         "list upload");
+    B_CK(b, cudaMemcpyAsync(b->d_list64 + m, fb.data(), sizeof(int) * fb.size(), cudaMemcpyHostToDevice, b->stream),
+         "fill list upload");
+    B_CK(b, cudaMemcpyAsync(b->d_list64 + 2 * m + 1, tb.data(), sizeof(int) * tb.size(), cudaMemcpyHostToDevice,
+                            b->stream), "tile list upload");
+  }
+  b->list64 = list;
+  b->total_fill = nf;
+  b->total_tiles = nt;
   return E2D_OK;
 }
 
@@ -153,7 +205,7 @@ int rebuild_list(e2d_batch *b) {
     bool all_min = true;
     for (int k = 0; k < b->max_inst; ++k) {
       HostInst &h = b->slots[k];
-      if (!h.used || !h.mirror.active) continue;
+      if (!h.used || h.fp64 || !h.mirror.active) continue;
       KParams32 kp = h.mirror.kp;
       kp.strip_h = std::max(16, ((b->strip_h[h.size_class] >> shift) / 16) * 16);
       all_min &= kp.strip_h == 16;
@@ -164,7 +216,7 @@ int rebuild_list(e2d_batch *b) {
   int total = 0;
   for (int k = 0; k < b->max_inst; ++k) {
     HostInst &h = b->slots[k];
-    if (!h.used || !h.mirror.active) continue;
+    if (!h.used || h.fp64 || !h.mirror.active) continue;
     const int sh = std::max(16, ((b->strip_h[h.size_class] >> shift) / 16) * 16);
     if (h.mirror.kp.strip_h != sh) {
       h.mirror.kp.strip_h = sh;
@@ -185,6 +237,10 @@ int rebuild_list(e2d_batch *b) {
     B_CK(b, cudaMemcpyAsync(b->d_list + b->max_inst, begin.data(), sizeof(int) * begin.size(),
                             cudaMemcpyHostToDevice, b->stream), "strip list upload");
   }
+  {
+    const int rc = rebuild_list64(b);
+    if (rc != E2D_OK) return rc;
+  }
   B_CK(b, cudaStreamSynchronize(b->stream), "list sync");
   b->list = list;
   b->total_strips = total;
@@ -201,9 +257,15 @@ int launch_iterations(e2d_batch *b, int iterations) {
     cudaGraph_t graph;
     B_CK(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "capture");
     cudaError_t le = cudaSuccess;
-    for (int k = 0; k < iterations && le == cudaSuccess; ++k)
-      le = launch_batch_f32c(b->riemann, b->variant, b->d_insts, b->d_list, b->d_list + b->max_inst,
-                             (int)b->list.size(), b->total_strips, b->grid, b->stream);
+    const int m = b->max_inst;
+    for (int k = 0; k < iterations && le == cudaSuccess; ++k) {
+      if (!b->list.empty())
+        le = launch_batch_f32c(b->riemann, b->variant, b->d_insts, b->d_list, b->d_list + m, (int)b->list.size(),
+                               b->total_strips, b->grid, b->stream);
+      if (le == cudaSuccess && !b->list64.empty())
+        le = launch_batch_f64(b->riemann, b->d_insts64, b->d_list64, b->d_list64 + m, b->d_list64 + 2 * m + 1,
+                              (int)b->list64.size(), b->total_fill, b->total_tiles, b->stream);
+    }
     cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
     if (le != cudaSuccess || ee != cudaSuccess) return berr(b, E2D_ECUDA, "batch capture");
     cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
@@ -214,6 +276,57 @@ int launch_iterations(e2d_batch *b, int iterations) {
     exec = it->second;
   }
   B_CK(b, cudaGraphLaunch(exec, b->stream), "batch launch");
+  return E2D_OK;
+}
+
+// An FP64 instance: U (initial state from the host or the device
+// initialiser), U2 = U, the primitive array; bit-identical to the single
+// FP64 path step for step.
+int admit64(e2d_batch *b, const e2d_params &p, double t_end, const double *u0, int slot, int *id) {
+  KParams64 kp;
+  make_kparams(p, &kp);
+  const size_t need = inst_bytes64(kp.g);
+  size_t off = 0;
+  if (!b->alloc.alloc(need, &off)) return berr(b, E2D_ENOMEM, "admit: pool full");
+  double *u0d = reinterpret_cast<double *>(b->pool + off);
+  double *u1d = u0d + 4 * kp.g.plane;
+  double *qd = u1d + 4 * kp.g.plane;
+  const size_t state_bytes = sizeof(double) * 4 * (size_t)kp.g.plane;
+  auto undo = [&](int st, const char *m) {
+    cudaStreamSynchronize(b->stream);
+    b->alloc.release(off, need);
+    return berr(b, st, m);
+  };
+  if (u0) {
+    if (cudaMemcpyAsync(u0d, u0, state_bytes, cudaMemcpyHostToDevice, b->stream) != cudaSuccess)
+      return undo(E2D_ECUDA, "admit: upload");
+  } else if (launch_init_f64(kp, p, u0d, b->stream) != cudaSuccess) {
+    return undo(E2D_ECUDA, "admit: init");
+  }
+  if (cudaMemcpyAsync(u1d, u0d, state_bytes, cudaMemcpyDeviceToDevice, b->stream) != cudaSuccess)
+    return undo(E2D_ECUDA, "admit: copy");
+  BatchInst64 I{};
+  I.kp = kp;
+  I.u[0] = u0d;
+  I.u[1] = u1d;
+  I.q = qd;
+  I.t = 0.0;
+  I.t_end = t_end;
+  I.active = I.t < I.t_end;
+  batch_f64_shape(kp, &I.nbx, &I.nfill, &I.ntx, &I.ntiles);
+  HostInst &h = b->slots[slot];
+  if (cudaMemcpyAsync(&b->d_insts64[slot], &I, sizeof(I), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return undo(E2D_ECUDA, "admit: table upload");
+  h.used = true;
+  h.fp64 = true;
+  h.p = p;
+  h.off = off;
+  h.bytes = need;
+  h.size_class = size_class_of(p.nx, p.ny);
+  h.mirror64 = I;
+  b->list_dirty = true;
+  *id = slot;
   return E2D_OK;
 }
 
@@ -239,8 +352,12 @@ int e2d_batch_create(int riemann, size_t pool_bytes, int max_instances, e2d_batc
   b->alloc.reset(pool_bytes);
   if (cudaMalloc(&b->d_insts, sizeof(BatchInst) * (size_t)max_instances) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&b->d_list, sizeof(int) * (2 * (size_t)max_instances + 1)) != cudaSuccess) return fail(E2D_ENOMEM);
-  if (cudaMemsetAsync(b->d_insts, 0, sizeof(BatchInst) * (size_t)max_instances, b->stream) != cudaSuccess)
+  if (cudaMalloc(&b->d_insts64, sizeof(BatchInst64) * (size_t)max_instances) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMalloc(&b->d_list64, sizeof(int) * (3 * (size_t)max_instances + 2)) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMemsetAsync(b->d_insts, 0, sizeof(BatchInst) * (size_t)max_instances, b->stream) != cudaSuccess ||
+      cudaMemsetAsync(b->d_insts64, 0, sizeof(BatchInst64) * (size_t)max_instances, b->stream) != cudaSuccess)
     return fail(E2D_ECUDA);
+  if (configure_f64_kernels() != cudaSuccess) return fail(E2D_ECUDA);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(E2D_ECUDA);
   *out = b;
   return E2D_OK;
@@ -253,6 +370,8 @@ int e2d_batch_destroy(e2d_batch *b) {
   if (b->pool) cudaFree(b->pool);
   if (b->d_insts) cudaFree(b->d_insts);
   if (b->d_list) cudaFree(b->d_list);
+  if (b->d_insts64) cudaFree(b->d_insts64);
+  if (b->d_list64) cudaFree(b->d_list64);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return E2D_OK;
@@ -273,6 +392,7 @@ size_t e2d_batch_instance_bytes(const e2d_params *pin) {
   if (params_init(&p, nullptr) != E2D_OK) return 0;
   KParams32 kp;
   make_kparams32(p, &kp);
+  if (p.precision == E2D_PRECISION_FP64) return PoolAllocator::round(inst_bytes64(kp.g));
   return PoolAllocator::round(inst_bytes(kp)) + PoolAllocator::round(sizeof(double) * 4 * (size_t)kp.g.plane);
 }
 
@@ -289,6 +409,7 @@ int e2d_batch_admit(e2d_batch *b, const e2d_params *pin, double t_end, const dou
       break;
     }
   if (slot < 0) return berr(b, E2D_ENOMEM, "admit: no free instance slot");
+  if (p.precision == E2D_PRECISION_FP64) return admit64(b, p, t_end, u0, slot, id);
   KParams32 kp;
   make_kparams32(p, &kp);
   const int cls = size_class_of(p.nx, p.ny);
@@ -343,6 +464,7 @@ int e2d_batch_admit(e2d_batch *b, const e2d_params *pin, double t_end, const dou
     return undo(E2D_ECUDA, "admit: sync");
   b->alloc.release(soff, stage_bytes);
   h.used = true;
+  h.fp64 = false;
   h.p = p;
   h.off = off;
   h.bytes = need;
@@ -359,7 +481,9 @@ int e2d_batch_release(e2d_batch *b, int id) {
   b->alloc.release(h.off, h.bytes);
   h.used = false;
   BatchInst zero{};
+  BatchInst64 zero64{};
   B_CK(b, cudaMemcpyAsync(&b->d_insts[id], &zero, sizeof(zero), cudaMemcpyHostToDevice, b->stream), "release");
+  B_CK(b, cudaMemcpyAsync(&b->d_insts64[id], &zero64, sizeof(zero64), cudaMemcpyHostToDevice, b->stream), "release");
   B_CK(b, cudaStreamSynchronize(b->stream), "release sync");
   b->list_dirty = true;
   return E2D_OK;
@@ -367,11 +491,11 @@ int e2d_batch_release(e2d_batch *b, int id) {
 
 int e2d_batch_query(e2d_batch *b, int id, double *t, int *nstep, int *active) {
   if (!b || id < 0 || id >= b->max_inst || !b->slots[id].used) return E2D_EINVAL;
-  const BatchInst &m = b->slots[id].mirror;
-  if (t) *t = m.t;
-  if (nstep) *nstep = m.nstep;
-  if (active) *active = m.active;
-  if (m.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT)) return berr(b, E2D_ENUMERIC, "instance hit NaN/Inf or a bad dt");
+  const HostInst &m = b->slots[id];
+  if (t) *t = m.t();
+  if (nstep) *nstep = m.nstep();
+  if (active) *active = m.active();
+  if (m.status() & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT)) return berr(b, E2D_ENUMERIC, "instance hit NaN/Inf or a bad dt");
   return E2D_OK;
 }
 
@@ -380,6 +504,12 @@ int e2d_batch_get_state(e2d_batch *b, int id, double *host, int layout) {
   if (layout != E2D_LAYOUT_LEFT) return berr(b, E2D_EINVAL, "batch get_state: LayoutLeft only");
   HostInst &h = b->slots[id];
   B_CK(b, cudaStreamSynchronize(b->stream), "get sync");
+  if (h.fp64) {
+    const size_t bytes = sizeof(double) * 4 * (size_t)h.mirror64.kp.g.plane;
+    B_CK(b, cudaMemcpyAsync(host, h.mirror64.u[h.mirror64.par], bytes, cudaMemcpyDeviceToHost, b->stream), "get_state");
+    B_CK(b, cudaStreamSynchronize(b->stream), "get_state");
+    return E2D_OK;
+  }
   const KParams32 kp = h.mirror.kp;
   const size_t stage_bytes = sizeof(double) * 4 * (size_t)kp.g.plane;
   size_t soff = 0;
@@ -399,23 +529,25 @@ int e2d_batch_run(e2d_batch *b, int iterations, int *n_active) {
     int rc = rebuild_list(b);
     if (rc != E2D_OK) return rc;
   }
-  if (!b->list.empty() && iterations > 0) {
+  if ((!b->list.empty() || !b->list64.empty()) && iterations > 0) {
     int rc = launch_iterations(b, iterations);
     if (rc != E2D_OK) return rc;
   }
   std::vector<int> before(b->max_inst);
-  for (int k = 0; k < b->max_inst; ++k) before[k] = b->slots[k].mirror.nstep;
+  for (int k = 0; k < b->max_inst; ++k) before[k] = b->slots[k].nstep();
   int rc = sync_mirrors(b);
   if (rc != E2D_OK) return rc;
   int active = 0;
   for (int k = 0; k < b->max_inst; ++k) {
     HostInst &h = b->slots[k];
     if (!h.used) continue;
-    b->cell_updates += (long long)(h.mirror.nstep - before[k]) * h.p.nx * h.p.ny;
-    if (h.mirror.active) ++active;
+    b->cell_updates += (long long)(h.nstep() - before[k]) * h.p.nx * h.p.ny;
+    if (h.active()) ++active;
   }
   for (int k : b->list)
-    if (!b->slots[k].mirror.active) b->list_dirty = true;
+    if (!b->slots[k].active()) b->list_dirty = true;
+  for (int k : b->list64)
+    if (!b->slots[k].active()) b->list_dirty = true;
   if (n_active) *n_active = active;
   return E2D_OK;
 }
@@ -509,7 +641,7 @@ int e2d_batch_autotune(e2d_batch *b, int iters_per_trial) {
   static const int cand[3] = {16, 32, 64};
   for (int c = 0; c < 3 && rc == E2D_OK; ++c) {
     bool present = false;
-    for (auto &h : b->slots) present |= h.used && h.mirror.active && h.size_class == c;
+    for (auto &h : b->slots) present |= h.used && !h.fp64 && h.mirror.active && h.size_class == c;
     if (!present) continue;
     int best_h = b->strip_h[c];
     double bm = 1e30;

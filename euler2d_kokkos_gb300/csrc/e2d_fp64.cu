@@ -283,69 +283,70 @@ __device__ __forceinline__ void riemann(const KPhys<double> &ph, const double *q
 }
 
 // ------------------------------------------------------------ kernel 1
-// Ghost fill + primitives + CFL maximum (see the file comment).
-__global__ void __launch_bounds__(FILL_BX *FILL_BY)
-    k_fill_f64(const KParams64 kp, double *__restrict__ u_in, double *__restrict__ u_out,
-               double *__restrict__ q, DevClock *clk, const int mode) {
-  if ((mode & FILL_DEVICE_CLOCK) && !(clk->t < clk->t_end)) return;
+// Ghost fill + primitives + CFL term of array cell (i, j) (see the file
+// comment); `term`/`flags` receive its CFL term and E2D_FLAG_* bits.
+__device__ __forceinline__ void fill_cell(const KParams64 &kp, double *__restrict__ u_in,
+                                          double *__restrict__ u_out, double *__restrict__ q,
+                                          const int mode, const int i, const int j, double &term,
+                                          unsigned int &flags) {
   const KGeom &g = kp.g;
   const KPhys<double> &ph = kp.ph;
-  const int i = blockIdx.x * FILL_BX + threadIdx.x;
-  const int j = blockIdx.y * FILL_BY + threadIdx.y;
-  double term = 0.0;
-  unsigned int flags = 0;
-  if (i < g.isize && j < g.jsize) {
-    bool fu, fv;
-    const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
-    const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
-    const bool ghost = (si != i) || (sj != j);
-    const size_t s = (size_t)si + (size_t)g.isize * sj;
-    const double rho = u_in[s];
-    const double e = u_in[s + g.plane];
-    double mx = u_in[s + 2 * g.plane];
-    double my = u_in[s + 3 * g.plane];
-    if (fu) mx = -mx;
-    if (fv) my = -my;
-    const size_t d = (size_t)i + (size_t)g.isize * j;
-    if (ghost) {
-      if (mode & FILL_GHOSTS_IN) {
-        u_in[d] = rho;
-        u_in[d + g.plane] = e;
-        u_in[d + 2 * g.plane] = mx;
-        u_in[d + 3 * g.plane] = my;
-      }
-      if (mode & FILL_GHOSTS_OUT) {
-        u_out[d] = rho;
-        u_out[d + g.plane] = e;
-        u_out[d + 2 * g.plane] = mx;
-        u_out[d + 3 * g.plane] = my;
-      }
+  if (i >= g.isize || j >= g.jsize) return;
+  bool fu, fv;
+  const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
+  const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
+  const bool ghost = (si != i) || (sj != j);
+  const size_t s = (size_t)si + (size_t)g.isize * sj;
+  const double rho = u_in[s];
+  const double e = u_in[s + g.plane];
+  double mx = u_in[s + 2 * g.plane];
+  double my = u_in[s + 3 * g.plane];
+  if (fu) mx = -mx;
+  if (fv) my = -my;
+  const size_t d = (size_t)i + (size_t)g.isize * j;
+  if (ghost) {
+    if (mode & FILL_GHOSTS_IN) {
+      u_in[d] = rho;
+      u_in[d + g.plane] = e;
+      u_in[d + 2 * g.plane] = mx;
+      u_in[d + 3 * g.plane] = my;
     }
-    if (mode & (FILL_WRITE_Q | FILL_DT)) {
-      double dd, p, ux, uy;
-      primitives(ph, rho, e, mx, my, dd, p, ux, uy);
-      if (mode & FILL_WRITE_Q) {
-        q[d] = dd;
-        q[d + g.plane] = p;
-        q[d + 2 * g.plane] = ux;
-        q[d + 3 * g.plane] = uy;
-      }
-      if ((mode & FILL_DT) && !ghost) {
-        // src/HydroRunFunctors.h:56-72
-        const double c = sqrt(ph.gamma0 * p / dd);
-        const double vx = c + fabs(ux);
-        const double vy = c + fabs(uy);
-        // vx / dx + vy / dy, as a product when the divisor is a power of two
-        const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
-        const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
-        term = tx + ty;
-        if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) flags |= E2D_FLAG_NONFINITE;
-        if (!(rho > 0.0)) flags |= E2D_FLAG_DENSITY;
-      }
+    if (mode & FILL_GHOSTS_OUT) {
+      u_out[d] = rho;
+      u_out[d + g.plane] = e;
+      u_out[d + 2 * g.plane] = mx;
+      u_out[d + 3 * g.plane] = my;
     }
   }
-  if (!(mode & FILL_DT)) return;
-  // block max of the CFL term (fmax drops NaN like the reference's reducer)
+  if (mode & (FILL_WRITE_Q | FILL_DT)) {
+    double dd, p, ux, uy;
+    primitives(ph, rho, e, mx, my, dd, p, ux, uy);
+    if (mode & FILL_WRITE_Q) {
+      q[d] = dd;
+      q[d + g.plane] = p;
+      q[d + 2 * g.plane] = ux;
+      q[d + 3 * g.plane] = uy;
+    }
+    if ((mode & FILL_DT) && !ghost) {
+      // src/HydroRunFunctors.h:56-72
+      const double c = sqrt(ph.gamma0 * p / dd);
+      const double vx = c + fabs(ux);
+      const double vy = c + fabs(uy);
+      // vx / dx + vy / dy, as a product when the divisor is a power of two
+      const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
+      const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
+      term = tx + ty;
+      if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) flags |= E2D_FLAG_NONFINITE;
+      if (!(rho > 0.0)) flags |= E2D_FLAG_DENSITY;
+    }
+  }
+}
+
+// Block maximum of the CFL term into *acc (fmax drops NaN like the
+// reference's reducer; positive doubles order like their bit patterns) and
+// the OR of the flags into *status.  Every thread of the block calls it.
+__device__ __forceinline__ void fill_reduce(double term, unsigned int flags, unsigned long long *acc,
+                                            unsigned int *status) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) term = fmax(term, __shfl_xor_sync(0xffffffffu, term, off));
   flags = __reduce_or_sync(0xffffffffu, flags);
@@ -364,10 +365,20 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
       m = fmax(m, wmax[w]);
       f |= wflags[w];
     }
-    // positive doubles order like their bit patterns
-    if (m > 0.0) atomicMax(&clk->invdt_bits, (unsigned long long)__double_as_longlong(m));
-    if (f) atomicOr(&clk->status, f);
+    if (m > 0.0) atomicMax(acc, (unsigned long long)__double_as_longlong(m));
+    if (f) atomicOr(status, f);
   }
+}
+
+__global__ void __launch_bounds__(FILL_BX *FILL_BY)
+    k_fill_f64(const KParams64 kp, double *__restrict__ u_in, double *__restrict__ u_out,
+               double *__restrict__ q, DevClock *clk, const int mode) {
+  if ((mode & FILL_DEVICE_CLOCK) && !(clk->t < clk->t_end)) return;
+  double term = 0.0;
+  unsigned int flags = 0;
+  fill_cell(kp, u_in, u_out, q, mode, blockIdx.x * FILL_BX + threadIdx.x, blockIdx.y * FILL_BY + threadIdx.y,
+            term, flags);
+  if (mode & FILL_DT) fill_reduce(term, flags, &clk->invdt_bits, &clk->status);
 }
 
 // ------------------------------------------------------------ kernel 2
@@ -377,56 +388,37 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
 // 2.09).  Measured on the 4096^2 blast: 15.12 and 15.38 ms per step; smaller
 // tiles (16 x 16, 32 x 8: 16.1, 16.7 ms) lose more to halo work than they
 // gain in residency.  Results do not depend on the shape.
-template <int RS, int TX, int TY, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-    k_flux_update_f64(const KParams64 kp, const double *__restrict__ q,
-                      const double *__restrict__ u_in, double *__restrict__ u_out, DevClock *clk,
-                      const int use_clock, const double host_dt, double *__restrict__ dt_trace) {
+// dt of a step from the CFL maximum (src/main.cpp:128-134).
+__device__ __forceinline__ double step_dt(const KPhys<double> &ph, unsigned long long invdt_bits, double t,
+                                          double t_end) {
+  const double inv_dt = __longlong_as_double((long long)invdt_bits);
+  double dt = ph.cfl / inv_dt;
+  if (t + dt > t_end) dt = t_end - t;
+  return dt;
+}
+
+// Stages 1-4 of the step for tile (bx, by) of a grid, block-wide; the
+// caller provides dt/dx, dt/dy and TX x TY shared memory.
+template <int RS, int TX, int TY, int NT>
+__device__ __forceinline__ void flux_tile(const KParams64 &kp, const double *__restrict__ q,
+                                          const double *__restrict__ u_in, double *__restrict__ u_out,
+                                          const int bx, const int by, const double dtdx, const double dtdy,
+                                          double *smem) {
   constexpr int QW = TX + 4;  // primitives tile width (2-cell halo)
   constexpr int QH = TY + 4;
   constexpr int XW = TX + 2;  // x-face states: cells x in [-1, TX]
   constexpr int YH = TY + 2;  // y-face states: cells y in [-1, TY]
-  extern __shared__ double smem[];
   double *sQ = smem;                   // [4][QH][QW]  primitives with halo
   double *sXm = sQ + 4 * QH * QW;      // [4][TY][XW]  XMIN states, then x-fluxes
   double *sXp = sXm + 4 * TY * XW;     // [4][TY][XW]  XMAX states
   double *sYm = sXp + 4 * TY * XW;     // [4][YH][TX]  YMIN states, then y-fluxes
   double *sYp = sYm + 4 * YH * TX;     // [4][YH][TX]  YMAX states
-
   const KGeom &g = kp.g;
   const KPhys<double> &ph = kp.ph;
   const int tid = threadIdx.x;
 
-  // dt of this step: the caller's, or src/main.cpp:128-134 on the device
-  // dt of this step (src/main.cpp:128-134 on the device) and dt/dx, dt/dy,
-  // computed once per block and broadcast: per-thread FP64 divisions here
-  // would cost ~2 divisions per cell on the FP64 pipe
-  __shared__ double s_dt[3];
-  __shared__ int s_run;
-  if (tid == 0) {
-    double dt = host_dt;
-    int run = 1;
-    if (use_clock) {
-      const double t = clk->t;
-      const double t_end = clk->t_end;
-      run = t < t_end;
-      const double inv_dt = __longlong_as_double((long long)clk->invdt_bits);
-      dt = ph.cfl / inv_dt;
-      if (t + dt > t_end) dt = t_end - t;
-    }
-    s_dt[0] = dt;
-    s_dt[1] = dt / ph.dx;
-    s_dt[2] = dt / ph.dy;
-    s_run = run;
-  }
-  __syncthreads();
-  if (!s_run) return;
-  const double dt = s_dt[0];
-  const double dtdx = s_dt[1];
-  const double dtdy = s_dt[2];
-
-  const int i0 = blockIdx.x * TX;  // array column of the tile's first halo cell
-  const int j0 = blockIdx.y * TY;
+  const int i0 = bx * TX;  // array column of the tile's first halo cell
+  const int j0 = by * TY;
 
   // stage 1: primitives of the tile and its 2-cell halo
   for (int k = tid; k < QH * QW; k += NT) {
@@ -542,6 +534,38 @@ __global__ void __launch_bounds__(NT, MINB)
     }
   }
 
+}
+
+template <int RS, int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_flux_update_f64(const KParams64 kp, const double *__restrict__ q,
+                      const double *__restrict__ u_in, double *__restrict__ u_out, DevClock *clk,
+                      const int use_clock, const double host_dt, double *__restrict__ dt_trace) {
+  extern __shared__ double smem[];
+  const KPhys<double> &ph = kp.ph;
+  const int tid = threadIdx.x;
+  // dt of this step (the caller's, or src/main.cpp:128-134 on the device)
+  // and dt/dx, dt/dy, computed once per block and broadcast: per-thread FP64
+  // divisions here would cost ~2 divisions per cell on the FP64 pipe
+  __shared__ double s_dt[3];
+  __shared__ int s_run;
+  if (tid == 0) {
+    double dt = host_dt;
+    int run = 1;
+    if (use_clock) {
+      run = clk->t < clk->t_end;
+      dt = step_dt(ph, clk->invdt_bits, clk->t, clk->t_end);
+    }
+    s_dt[0] = dt;
+    s_dt[1] = dt / ph.dx;
+    s_dt[2] = dt / ph.dy;
+    s_run = run;
+  }
+  __syncthreads();
+  if (!s_run) return;
+  const double dt = s_dt[0];
+  flux_tile<RS, TX, TY, NT>(kp, q, u_in, u_out, blockIdx.x, blockIdx.y, s_dt[1], s_dt[2], smem);
+
   if (!use_clock) return;
   // the last block to finish advances the loop state (src/main.cpp:139-143)
   __syncthreads();
@@ -560,6 +584,82 @@ __global__ void __launch_bounds__(NT, MINB)
       clk->nstep = ns + 1;
       clk->invdt_bits = 0ull;
       clk->done_blocks = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------------ batches
+// Instance k of a work list with begin[k] <= w < begin[k + 1].
+__device__ __forceinline__ int list_entry(const int *__restrict__ begin, int n, int w) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (begin[mid] <= w)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// The fill pass of one iteration for every listed FP64 instance: one block
+// per fill block of an instance (the single-grid k_fill_f64 with the device
+// clock's mode), the CFL maximum into the instance's accumulator.
+__global__ void __launch_bounds__(FILL_BX *FILL_BY)
+    k_batch_fill_f64(BatchInst64 *__restrict__ insts, const int *__restrict__ list_slots,
+                     const int *__restrict__ fill_begin, const int n_inst) {
+  const int k = list_entry(fill_begin, n_inst, blockIdx.x);
+  BatchInst64 &I = insts[list_slots[k]];
+  if (!I.active) return;  // block-uniform
+  const int b = blockIdx.x - fill_begin[k];
+  const int by = b / I.nbx, bx = b - by * I.nbx;
+  const int par = I.par;
+  double term = 0.0;
+  unsigned int flags = 0;
+  fill_cell(I.kp, I.u[par], I.u[par ^ 1], I.q, FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT,
+            bx * FILL_BX + threadIdx.x, by * FILL_BY + threadIdx.y, term, flags);
+  fill_reduce(term, flags, &I.acc, &I.status);
+}
+
+// The flux pass: one 32 x 32 tile per block with its instance's dt; the
+// instance's last tile advances its loop state (src/main.cpp:139-143).
+template <int RS>
+__global__ void __launch_bounds__(512, 1)
+    k_batch_flux_f64(BatchInst64 *__restrict__ insts, const int *__restrict__ list_slots,
+                     const int *__restrict__ tile_begin, const int n_inst) {
+  extern __shared__ double smem[];
+  const int k = list_entry(tile_begin, n_inst, blockIdx.x);
+  BatchInst64 &I = insts[list_slots[k]];
+  if (!I.active) return;  // block-uniform
+  const KPhys<double> &ph = I.kp.ph;
+  __shared__ double s_dt[3];
+  if (threadIdx.x == 0) {
+    const double dt = step_dt(ph, I.acc, I.t, I.t_end);
+    s_dt[0] = dt;
+    s_dt[1] = dt / ph.dx;
+    s_dt[2] = dt / ph.dy;
+  }
+  __syncthreads();
+  const int b = blockIdx.x - tile_begin[k];
+  const int by = b / I.ntx, bx = b - by * I.ntx;
+  const int par = I.par;
+  flux_tile<RS, 32, 32, 512>(I.kp, I.q, I.u[par], I.u[par ^ 1], bx, by, s_dt[1], s_dt[2], smem);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&I.done, 1u);
+    if (ticket == (unsigned)I.ntiles - 1u) {
+      __threadfence();
+      const double dt = s_dt[0];
+      if (!(dt > 0.0) || nonfinite(dt)) I.status |= E2D_FLAG_BAD_DT;
+      I.dt = dt;
+      I.t = I.t + dt;
+      I.nstep = I.nstep + 1;
+      I.par = par ^ 1;
+      I.acc = 0ull;
+      I.done = 0u;
+      I.active = (I.t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
       __threadfence();
     }
   }
@@ -738,11 +838,46 @@ static cudaError_t configure_rs() {
   return e;
 }
 
+template <int RS>
+static cudaError_t set_batch_flux_smem() {
+  return cudaFuncSetAttribute(k_batch_flux_f64<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)flux_smem_bytes<32, 32>());
+}
+
 cudaError_t configure_f64_kernels() {
   cudaError_t e = configure_rs<E2D_RIEMANN_HLLC>();
   if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_HLL>();
   if (e == cudaSuccess) e = configure_rs<E2D_RIEMANN_APPROX>();
+  if (e == cudaSuccess) e = set_batch_flux_smem<E2D_RIEMANN_HLLC>();
+  if (e == cudaSuccess) e = set_batch_flux_smem<E2D_RIEMANN_HLL>();
+  if (e == cudaSuccess) e = set_batch_flux_smem<E2D_RIEMANN_APPROX>();
   return e;
+}
+
+void batch_f64_shape(const KParams64 &kp, int *nbx, int *nfill, int *ntx, int *ntiles) {
+  *nbx = (kp.g.isize + FILL_BX - 1) / FILL_BX;
+  *nfill = *nbx * ((kp.g.jsize + FILL_BY - 1) / FILL_BY);
+  *ntx = (kp.g.nx + 31) / 32;
+  *ntiles = *ntx * ((kp.g.ny + 31) / 32);
+}
+
+cudaError_t launch_batch_f64(int riemann, BatchInst64 *insts, const int *list_slots, const int *fill_begin,
+                             const int *tile_begin, int n_inst, int total_fill, int total_tiles, cudaStream_t s) {
+  if (n_inst <= 0 || total_fill <= 0 || total_tiles <= 0) return cudaSuccess;
+  k_batch_fill_f64<<<total_fill, dim3(FILL_BX, FILL_BY), 0, s>>>(insts, list_slots, fill_begin, n_inst);
+  const size_t sm = flux_smem_bytes<32, 32>();
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC:
+      k_batch_flux_f64<E2D_RIEMANN_HLLC><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      break;
+    case E2D_RIEMANN_HLL:
+      k_batch_flux_f64<E2D_RIEMANN_HLL><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      break;
+    default:
+      k_batch_flux_f64<E2D_RIEMANN_APPROX><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      break;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const double *q,

@@ -172,3 +172,31 @@ def test_device_initial_conditions_equal_host_generators(gpu_lib):
             run_to_end(b)
             outs.append(b.get_state(i))
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_batch_fp64_instances_equal_single_fp64_path(gpu_lib):
+    """FP64 instances of uneven size (with FP32C instances in the same
+    batch) each end bit for bit where the single FP64 path (bit-identical to
+    the reference) ends, after the same number of steps; the FP32C instances
+    are unchanged by the FP64 ones sharing their batch."""
+    fp64 = W.mixed_batch(4, seed=31, max_side=160, precision=e2d.PRECISION_FP64)
+    fp32 = small_mix(3, seed=32)
+    with e2d.Batch(pool_bytes=POOL) as b:
+        ids64 = [b.admit(s.params, s.t_end) for s in fp64]
+        ids32 = [b.admit(s.params, s.t_end) for s in fp32]
+        run_to_end(b)
+        got64 = [(b.get_state(i), b.query(i)) for i in ids64]
+        got32 = [b.get_state(i) for i in ids32]
+    for s, (u, (t, ns, active)) in zip(fp64, got64):
+        assert not active and t == s.t_end
+        with e2d.HydroRun(s.params) as h:
+            tt, n = 0.0, 0
+            while tt < s.t_end:
+                tt, n, _ = h.step_n(64, s.t_end, tt, n, want_trace=False)
+            assert (tt, n) == (t, ns)
+            assert np.array_equal(h.current(n), u)
+    for s, u in zip(fp32, got32):
+        with e2d.Batch(pool_bytes=POOL) as alone:
+            i = alone.admit(s.params, s.t_end)
+            run_to_end(alone)
+            assert np.array_equal(alone.get_state(i), u)
