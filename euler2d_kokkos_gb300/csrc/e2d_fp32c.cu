@@ -14,13 +14,15 @@
 // two adjacent columns, each warp a strip of 60 output columns (64 loaded:
 // the 2-column halo on each side) by strip_h rows, and walks down the strip one row
 // at a time keeping three rows of primitives, the previous row's face states
-// and fluxes in registers.  Neighbour columns come from warp shuffles; there
-// is no shared-memory staging and no block barrier in the march.  The two
-// columns of a lane are computed together with Blackwell's packed FP32
-// instructions (FFMA2 / FADD2 / FMUL2 on float2).  Ghost cells are read
-// through the boundary map, so no fill pass runs and ghost cells of the
-// arrays are never read.  Algorithmic traffic: 32 B read + 32 B written per
-// cell.
+// and fluxes in registers.  Neighbour columns come from warp shuffles, and
+// no block barrier is taken in the march.  Input rows reach the warp either
+// as register loads one row ahead or (default variants) through a per-warp
+// shared-memory ring filled by cp.async two rows ahead, ordered by one warp
+// barrier per row.  The two columns of a lane are computed together with
+// Blackwell's packed FP32 instructions (FFMA2 / FADD2 / FMUL2 on float2).
+// Ghost cells are read through the boundary map, so no fill pass runs and
+// ghost cells of the arrays are never read.  Algorithmic traffic: 32 B read
+// + 32 B written per cell.
 #include "e2d_common.cuh"
 #include "e2d_internal.h"
 
@@ -128,7 +130,8 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
   const float2 rstar = rs * sdu * isds;
   const float2 etotstar = fma2(ptotstar, ustar, fma2(sdu, es, neg2(ps * us))) * isds;
   // SL > 0: left state; else star (left or right); SR <= 0: right state.
-  // Supersonic faces are rare: a warp with none of them skips the selects.
+  // (no branch around the selects: the x and y solves of a row stay in one
+  // basic block)
   const bool sx = SL.x > 0.0f, sy = SL.y > 0.0f;
   const bool tx = !sx && (lx || SR.x > 0.0f), ty = !sy && (ly || SR.y > 0.0f);
   const float2 ro = sel2(sx, sy, rl, sel2(tx, ty, rstar, rr));
