@@ -383,8 +383,9 @@ class HydroRun:
 
 
 class Batch:
-    """Many independent FP32-compensated solves of uneven size in one device
-    pool, advanced together (e2d_batch_* in include/e2d.h)."""
+    """Many independent solves of uneven size (each FP32-compensated or FP64,
+    as its parameters say) in one device pool, advanced together
+    (e2d_batch_* in include/e2d.h)."""
 
     def __init__(self, riemann: str = "hllc", pool_bytes: int = 8 << 30, max_instances: int = 1024):
         self._lib = load_library()
@@ -449,6 +450,8 @@ class Batch:
         return t.value, ns.value, bool(a.value)
 
     def get_state(self, id: int) -> np.ndarray:
+        if id not in self.shapes:
+            raise E2DError(1, "get_state", f"instance {id} is not in the batch")  # E2D_EINVAL
         out = np.empty(self.shapes[id], dtype=np.float64)
         self._ck(self._lib.e2d_batch_get_state(self._h, int(id), out.ctypes.data, LAYOUT_LEFT), "get_state")
         return out

@@ -200,3 +200,26 @@ def test_batch_fp64_instances_equal_single_fp64_path(gpu_lib):
             i = alone.admit(s.params, s.t_end)
             run_to_end(alone)
             assert np.array_equal(alone.get_state(i), u)
+
+
+def test_batch_error_paths(gpu_lib):
+    s = small_mix(1, seed=41)[0]
+    with e2d.Batch(pool_bytes=POOL) as b:
+        p_hll = s.params.copy()
+        p_hll.riemannSolverType = e2d.RIEMANN["hll"]
+        with pytest.raises(e2d.E2DError) as ei:
+            b.admit(p_hll, s.t_end)  # the batch runs HLLC
+        assert ei.value.status == 1
+        for call in (lambda: b.query(3), lambda: b.get_state(3), lambda: b.release(3)):
+            with pytest.raises(e2d.E2DError) as ei:
+                call()  # slot 3 was never admitted
+            assert ei.value.status == 1
+        assert b.run(0) == 0  # nothing admitted: nothing active
+        i = b.admit(s.params, s.t_end)
+        assert b.run(0) == 1
+        b.release(i)
+        with pytest.raises(e2d.E2DError):
+            b.query(i)
+    with pytest.raises(e2d.E2DError) as ei:
+        e2d.Batch(pool_bytes=1 << 20, max_instances=0)
+    assert ei.value.status == 1

@@ -108,3 +108,23 @@ def test_fp32c_conservation_audit_fp64_matches_numpy(gpu_lib, tmp_path):
     ref = inner.sum(axis=1)
     # summation order differs from numpy's: bound by the sum of magnitudes
     assert np.all(np.abs(s - ref) <= 1e-13 * np.abs(inner).sum(axis=1)), (s, ref)
+
+
+@pytest.mark.parametrize("nx,ny,bc", [(2, 2, (1, 1, 1, 1)), (3, 5, (2, 2, 2, 2)), (7, 121, (3, 3, 1, 2)),
+                                      (59, 17, (1, 2, 3, 3)), (60, 16, (3, 3, 3, 3)),
+                                      (61, 33, (2, 1, 1, 2)), (121, 7, (1, 1, 2, 2)),
+                                      (122, 48, (3, 3, 2, 2))])
+def test_fp32c_edge_sizes(gpu_lib, tmp_path, nx, ny, bc):
+    """Grids narrower than a 60-column strip, with 1- or 2-column
+    remainders, shorter than a 16-row fold unit, and every boundary type on
+    the strips that read ghost columns and rows through the boundary map:
+    FP32C stays within the tolerance of FP64 and dt agrees to 1e-5."""
+    g14 = C.f32(1.4)
+    text = C.ini_text(nx, ny, bc=bc)
+    u0 = C.smooth_state(nx, ny, g14, seed=nx * 1000 + ny)
+    h64, h32 = pair(text, tmp_path, u0)
+    t64, n64, dt64 = h64.step_n(20, 10.0, 0.0, 0)
+    t32, n32, dt32 = h32.step_n(20, 10.0, 0.0, 0)
+    assert n64 == n32 == 20
+    assert np.allclose(dt32, dt64, rtol=1e-5, atol=0)
+    assert rel_l1(h32, n32 % 2, h64, n64 % 2) < FP32C_L1_TOL
