@@ -473,6 +473,9 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
                                             unsigned int *status, float *ring) {
+  // sum of the lane's new conserved values over the strip: NaN or infinite
+  // when one of them is (a sum that overflows FP32 reads as non-finite too)
+  float2 nfacc = f2(0.0f);
   float best = -1.0f;      // the lane's largest CFL term in the current fold unit
   int blocal = 0;          // and its strip-local index + 1 (0: none)
   float pend_term = 0.0f;  // lane u: the winner of the strip's fold unit u
@@ -677,6 +680,12 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
         if (target) {
           const float2 t = cfl_term2(k, idx, nh);
           const int loc = (m - 1 - rb) * 64 + 2 * lane + 1;
+          // non-finite states: a NaN term never wins the arg-max, and the
+          // primitives' fmaxf cut-offs drop a NaN density or energy, so the
+          // new conserved values themselves are summed (tested at strip end)
+          float2 chk = (nh[0] + nh[1]) + (nh[2] + nh[3]);
+          if (!(c0 + 1 < g.nx + 2)) chk.y = 0.0f;  // a ghost column: not a cell of the grid
+          nfacc = nfacc + chk;
           if (t.x > best) best = t.x, blocal = loc;
           if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, blocal = loc + 1;
         }
@@ -704,6 +713,9 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   }
   // the strip's fold-unit winners, one lane each, folded in parallel
   if (target) {
+    const float kInf = __int_as_float(0x7f800000);
+    const bool nonfin = !(fabsf(nfacc.x) < kInf) || !(fabsf(nfacc.y) < kInf);
+    if (__any_sync(0xffffffffu, nonfin) && lane == 0) atomicOr(status, (unsigned)E2D_FLAG_NONFINITE);
     __syncwarp();  // the winners were written by lanes of this warp
     if (pend_local > 0) {
       const int L = pend_local - 1;

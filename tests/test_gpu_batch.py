@@ -223,3 +223,27 @@ def test_batch_error_paths(gpu_lib):
     with pytest.raises(e2d.E2DError) as ei:
         e2d.Batch(pool_bytes=1 << 20, max_instances=0)
     assert ei.value.status == 1
+
+
+@pytest.mark.parametrize("precision", ["fp32c", "fp64"])
+def test_batch_nonfinite_instance_is_isolated(gpu_lib, precision):
+    """A solve whose state holds a NaN is stopped and reported (E2D_ENUMERIC
+    from query); the other solves of the batch finish as they do alone."""
+    prec = e2d.PRECISION_FP32C if precision == "fp32c" else e2d.PRECISION_FP64
+    good, bad = W.mixed_batch(2, seed=51, max_side=128, precision=prec, device_init=False)
+    u_bad = bad.u0.copy()
+    u_bad[0, 10, 10] = np.nan
+    with e2d.Batch(pool_bytes=POOL) as b:
+        ig = b.admit(good.params, good.t_end, good.u0)
+        ib = b.admit(bad.params, bad.t_end, u_bad)
+        run_to_end(b)
+        with pytest.raises(e2d.E2DError) as ei:
+            b.query(ib)
+        assert ei.value.status == 3  # E2D_ENUMERIC
+        t, ns, active = b.query(ig)
+        assert not active and t == good.t_end
+        mixed = b.get_state(ig)
+    with e2d.Batch(pool_bytes=POOL) as alone:
+        i = alone.admit(good.params, good.t_end, good.u0)
+        run_to_end(alone)
+        assert np.array_equal(alone.get_state(i), mixed)

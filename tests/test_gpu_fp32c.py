@@ -128,3 +128,16 @@ def test_fp32c_edge_sizes(gpu_lib, tmp_path, nx, ny, bc):
     assert n64 == n32 == 20
     assert np.allclose(dt32, dt64, rtol=1e-5, atol=0)
     assert rel_l1(h32, n32 % 2, h64, n64 % 2) < FP32C_L1_TOL
+
+
+def test_fp32c_nonfinite_state_reports_enumeric(gpu_lib, tmp_path):
+    """A NaN in the state stops the FP32C device loop with E2D_ENUMERIC, as
+    on the FP64 path."""
+    text = C.ini_text(64, 48, problem="implode")
+    _, h32 = pair(text, tmp_path)
+    u = h32.U
+    u[0, 20, 20] = np.nan
+    h32.set_state(0, u)
+    with pytest.raises(e2d.E2DError) as ei:
+        h32.step_n(10, 10.0, 0.0, 0)
+    assert ei.value.status == 3  # E2D_ENUMERIC
