@@ -278,7 +278,7 @@ int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
   p->blast_total_energy_inside = m.get_float("blast", "total_energy_inside", 0.0f);
   p->blast_nbins = (int)m.get_integer("blast", "nbins", 100);
 
-  // extensions of this build (absent keys keep the reference's behaviour)
+  // extension keys (absent keys keep the reference's behaviour)
   const std::string none = "\x01";
   auto opt_float = [&](const char *sec, const std::string &key, double dflt) {
     return m.get_string(sec, key, none) == none ? dflt : (double)m.get_float(sec, key, 0.0f);

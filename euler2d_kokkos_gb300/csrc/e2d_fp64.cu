@@ -171,8 +171,9 @@ __device__ __noinline__ void riemann_approx(const KPhys<double> &ph, const doubl
 }
 
 // src/HydroBaseFunctor.h:704-809 (riemann_hllc).  The reference builds the
-// star states of both sides and keeps one; this builds only the side the
-// contact selects (ustar > 0: left), which yields the same value.  Cut-offs,
+// star states of both sides and keeps one; here only the star state of the
+// side the contact selects (ustar > 0: left) is built, which yields the same
+// value.  Cut-offs,
 // maxima, the 0.5 factors and the sign tests use the exact integer forms of
 // e2d_f64_exact.cuh.
 __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const double *ql,

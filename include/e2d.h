@@ -225,11 +225,14 @@ int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double 
 
 /* ---------------------------------------------------------------------------
  * Batched solves.  No counterpart in the reference, which runs one grid per
- * process: this build's serving mode keeps many independent simulations of
+ * process: the serving mode here keeps many independent simulations of
  * uneven size resident in one device memory pool and advances all active
- * ones together, one kernel launch per iteration (each instance with its own
- * dt and t_end), replayed from CUDA graphs.  Arithmetic: FP32 compensated.
- * One Riemann solver per batch.  A handle is used from one host thread.
+ * ones together, one kernel launch per iteration for the FP32C instances and
+ * one fill + flux pair for the FP64 ones (each instance with its own dt and
+ * t_end), replayed from CUDA graphs.  Arithmetic: each instance's
+ * params.precision (FP64 instances end bit for bit where the single FP64
+ * path ends).  One Riemann solver per batch.  A handle is used from one host
+ * thread.
  * ------------------------------------------------------------------------- */
 typedef struct e2d_batch e2d_batch;
 /* A batch with a device pool of pool_bytes and room for max_instances. */
@@ -277,7 +280,7 @@ int e2d_batch_autotune(e2d_batch *b, int iters_per_trial);
  *                         -- trace_unsplit_2d_along_dir, :214-291
  *   E2D_EVAL_RIEMANN_*    in 8/item (qleft, qright)      out 4 (flux)
  *                         -- riemann_approx :558-693, riemann_hllc :704-809,
- *                            and the HLL flux this build adds.
+ *                            and the HLL flux (Toro eq. 10.21) added here.
  * dtdx / dtdy are used by the trace only. */
 enum {
   E2D_EVAL_PRIMITIVES = 0,

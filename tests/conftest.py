@@ -36,7 +36,7 @@ def kat(golden_dir):
 
 @pytest.fixture(scope="session")
 def gpu_lib():
-    """The CUDA library, required to load on a GPU machine (no fallback)."""
+    """The CUDA library, required to load where a GPU is visible (no fallback)."""
     import torch
 
     if not torch.cuda.is_available():

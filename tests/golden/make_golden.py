@@ -176,7 +176,7 @@ def gen_runs(R: ReferenceLib, tmp: str) -> dict:
 
 
 def gen_c1(R: ReferenceLib, tmp: str) -> dict:
-    """BASELINE's first configuration: implosion x+y>0.5, 256x256, gamma 1.4,
+    """The implosion benchmark configuration: x+y>0.5, 256x256, gamma 1.4,
     CFL 0.8, reflecting walls, HLLC, 1000 steps."""
     text = C.ini_text(256, 256, problem="implode", nStepmax=1000)
     path = C.write_ini(text, tmp, "c1.ini")
