@@ -112,3 +112,37 @@ def test_make_params_matches_ini(tmp_path):
     for f in ("nx", "ny", "isize", "jsize", "dx", "dy", "gamma0", "cfl", "smallp", "smallpp",
               "gamma6", "riemannSolverType", "boundary_type_xmax"):
         assert getattr(a, f) == getattr(b, f), f
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/e2d.h compiles as C11 (the boundary cgo, JNI and ctypes
+    callers bind), and the loop of INTEGRATION.md's C example type-checks."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_e2d.c"
+    src.write_text("""
+#include <stdlib.h>
+#include "e2d.h"
+int run(const char *ini) {
+  e2d_params p; e2d_sim *sim;
+  if (e2d_params_from_ini(ini, &p) != E2D_OK) return 1;
+  if (e2d_create(&p, &sim) != E2D_OK || e2d_init_problem(sim) != E2D_OK) return 2;
+  double t = 0; int nStep = 0;
+  int rc = e2d_step_n(sim, p.nStepmax, p.tEnd, &t, &nStep, NULL);
+  double *u = malloc(sizeof(double) * 4 * p.isize * p.jsize);
+  e2d_get_state(sim, nStep % 2, u, E2D_LAYOUT_LEFT);
+  e2d_batch *b;
+  if (e2d_batch_create(E2D_RIEMANN_HLLC, (size_t)1 << 30, 16, &b) == E2D_OK) e2d_batch_destroy(b);
+  free(u);
+  e2d_destroy(sim);
+  return rc;
+}
+""")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", "-I", inc, str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
