@@ -352,12 +352,12 @@ def fp64_pipe_info(kt, cells):
     return out
 
 
-def l1_check(e2d, nx, t_end):
-    """FP32C vs FP64 (bit-identical to the reference) on the four-quadrant
-    problem at nx^2 to t_end: relative L1 of density, FP64 accumulation."""
+def l1_check(e2d, nx, t_end, problem="four_quadrant"):
+    """FP32C vs FP64 (bit-identical to the reference) on the problem at nx^2
+    to t_end: relative L1 of density, FP64 accumulation."""
     hs = {}
     for prec in ("fp64", "fp32c"):
-        h = e2d.HydroRun(workload_params(e2d, "four_quadrant", nx, "hllc", prec))
+        h = e2d.HydroRun(workload_params(e2d, problem, nx, "hllc", prec))
         t, ns = 0.0, 0
         while t < t_end and ns < 1_000_000:
             t, ns, tr = h.step_n(512, t_end, t, ns)
@@ -548,6 +548,15 @@ def main():
             "ms_per_step": s["ms"] / args.steps,
             "roofline": roofline(s["kernels"], "fp32c", sc, "k_step_f32c"),
             "accuracy": l1_check(e2d, 1024, 0.3)}
+        # the C2 blast in the FP32 compensated mode, with its error against FP64
+        sb = measure(e2d, torch, args, "fp32c", args.problem, nx, args.steps, args.warmup, local,
+                     barrier, None, with_e2e=False, with_clocks=False)
+        line["fp32c_blast"] = {
+            "config": config(args.problem, nx, args.riemann, "fp32c"),
+            "value": cells * args.steps / (sb["ms"] / 1e3) / 1e9, "unit": METRIC,
+            "ms_per_step": sb["ms"] / args.steps,
+            "roofline": roofline(sb["kernels"], "fp32c", cells, "k_step_f32c"),
+            "accuracy": l1_check(e2d, 1024, 0.05, args.problem)}
         # C2 also names the HLL solver: the same FP64 blast with it
         hl = measure(e2d, torch, args, "fp64", args.problem, nx, args.steps, args.warmup, local,
                      barrier, None, with_e2e=False, with_clocks=False, riemann="hll")
