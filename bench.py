@@ -56,13 +56,16 @@ def parse():
                     help="steps of the CPU baseline sample (0: sized to ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve"],
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "c3"],
                     help="step: one grid (default); batch: 512 mixed solves batched vs one at a "
-                         "time; serve: Poisson arrivals into the batched loop")
+                         "time; serve: Poisson arrivals into the batched loop; c3: the 8192^2 "
+                         "four-quadrant problem to t = 0.3 in FP32C, in FP64 and in FP64 from a perturbed "
+                         "initial state (about 40 min at 8192^2, 5 min at 4096^2)")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--sample", type=int, default=24, help="solves timed one at a time (batch mode)")
     ap.add_argument("--rates", default="", help="arrival rates (solves/s) for serve mode, comma-separated")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--c3-nx", type=int, default=8192, help="grid side of --mode c3")
     a = ap.parse_args()
     if a.problem is None:
         a.problem = "blast" if a.precision == "fp64" else "four_quadrant"
@@ -482,6 +485,54 @@ def serve_mode(args):
     print(json.dumps(line), flush=True)
 
 
+def c3_mode(args):
+    """C3 at its full size: the four-quadrant problem (--c3-nx, 8192^2 by
+    default) run to t = 0.3 in FP32C and in FP64 (bit-identical to the
+    reference, the transitive oracle), plus a control: FP64 again from the
+    initial state multiplied by 1 + 1e-7 N(0, 1) (seed 0).  Reports the
+    relative L1 of density of FP32C and of the control against FP64: the
+    control measures how much this flow amplifies a perturbation of FP32's
+    size by t = 0.3."""
+    import torch
+
+    import euler2d_kokkos_gb300 as e2d
+
+    nx, t_end = args.c3_nx, 0.3
+    runs = {}
+    for prec in ("fp32c", "fp64", "fp64_control"):
+        h = e2d.HydroRun(workload_params(e2d, "four_quadrant", nx, "hllc", "fp32c" if prec == "fp32c" else "fp64"))
+        if prec == "fp64_control":
+            u = h.U
+            u = u * (1.0 + 1e-7 * np.random.default_rng(0).standard_normal(u.shape))
+            h.set_state(0, u)
+            h.set_state(1, u)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t, ns = 0.0, 0
+        while t < t_end:
+            prev = ns
+            t, ns, _ = h.step_n(1024, t_end, t, ns, want_trace=False)
+            if ns == prev:
+                break
+        torch.cuda.synchronize()
+        runs[prec] = (h, t, ns, time.perf_counter() - t0)
+    (h32, t32, n32, s32), (h64, t64, n64, s64) = runs["fp32c"], runs["fp64"]
+    hc, tc, nc, sc = runs["fp64_control"]
+    d, r = h32.l1_diff(n32 % 2, h64, n64 % 2, e2d.ID)
+    dc, rc = hc.l1_diff(nc % 2, h64, n64 % 2, e2d.ID)
+    line = mode_line(nx * nx * n32 / s32 / 1e9, "c3",
+                     {"workload": workload_name("four_quadrant", nx, "hllc", "fp32c") + f", to t = {t_end}"},
+                     {"fp32c": {"steps": n32, "t": t32, "seconds": s32, "gcell_per_s": nx * nx * n32 / s32 / 1e9},
+                      "fp64": {"steps": n64, "t": t64, "seconds": s64, "gcell_per_s": nx * nx * n64 / s64 / 1e9},
+                      "rel_l1_density_fp32c_vs_fp64": d / r,
+                      "rel_l1_density_control_vs_fp64": dc / rc,
+                      "control": "FP64 from the initial state times 1 + 1e-7 N(0,1)",
+                      "oracle": "FP64 GPU path (bit-identical to the reference)"})
+    for h, *_ in runs.values():
+        h.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -495,6 +546,10 @@ def main():
     if args.mode == "serve":
         if rank == 0:
             serve_mode(args)
+        return
+    if args.mode == "c3":
+        if rank == 0:
+            c3_mode(args)
         return
 
     import torch
