@@ -172,4 +172,51 @@ struct ComputeRadialProfileFunctor {
   }
 };
 
+// Batched solves (e2d_batch_* in e2d.h; no counterpart in the reference):
+// solves of uneven size, each FP32C or FP64 as its HydroParams say, resident
+// in one device pool and advanced together with per-solve dt and t_end.
+class Batch {
+ public:
+  explicit Batch(size_t pool_bytes, int max_instances = 1024, int riemann = E2D_RIEMANN_HLLC) {
+    check(e2d_batch_create(riemann, pool_bytes, max_instances, &b_), "Batch");
+  }
+  Batch(const Batch &) = delete;
+  Batch &operator=(const Batch &) = delete;
+  ~Batch() {
+    if (b_) e2d_batch_destroy(b_);
+  }
+  // admit a solve: u0 (LayoutLeft FP64, ghosts included) or nullptr to build
+  // the parameters' initial condition on the device; returns its id
+  int admit(const HydroParams &p, double t_end, const double *u0 = nullptr) {
+    int id = -1;
+    ck(e2d_batch_admit(b_, &p, t_end, u0, &id), "Batch::admit");
+    return id;
+  }
+  // advance every active solve; returns how many are still active
+  int run(int iterations) {
+    int n = 0;
+    ck(e2d_batch_run(b_, iterations, &n), "Batch::run");
+    return n;
+  }
+  bool active(int id, double *t = nullptr, int *nstep = nullptr) {
+    int a = 0;
+    ck(e2d_batch_query(b_, id, t, nstep, &a), "Batch::query");
+    return a != 0;
+  }
+  std::vector<double> state(int id, const HydroParams &p) {
+    std::vector<double> u((size_t)4 * p.isize * p.jsize);
+    ck(e2d_batch_get_state(b_, id, u.data(), E2D_LAYOUT_LEFT), "Batch::get_state");
+    return u;
+  }
+  void release(int id) { ck(e2d_batch_release(b_, id), "Batch::release"); }
+  void autotune(int iters_per_trial = 2) { ck(e2d_batch_autotune(b_, iters_per_trial), "Batch::autotune"); }
+  e2d_batch *handle() { return b_; }
+
+ private:
+  void ck(int status, const char *what) {
+    if (status != E2D_OK) throw Error(status, std::string(what) + " (" + e2d_batch_last_error(b_) + ")");
+  }
+  e2d_batch *b_ = nullptr;
+};
+
 }  // namespace euler2d_gb300

@@ -146,3 +146,49 @@ int run(const char *ini) {
     r = subprocess.run([cc, "-std=c11", "-Wall", "-Werror", "-fsyntax-only", "-I", inc, str(src)],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_mirror_compiles(tmp_path):
+    """include/euler2d_gb300.hpp (the C++ mirror of ConfigMap, HydroParams,
+    HydroRun, the radial profile and batches) compiles as C++17 with the
+    reference's driver loop written against it."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "use_mirror.cpp"
+    src.write_text("""
+#include "euler2d_gb300.hpp"
+using namespace euler2d_gb300;
+int main(int argc, char **argv) {
+  ConfigMap configMap(argv[1]);
+  HydroParams params;
+  params.setup(configMap);
+  HydroRun hydro(params, configMap);
+  double t = 0, dt = hydro.compute_dt(0);
+  int nStep = 0;
+  hydro.make_boundaries(hydro.U);
+  hydro.make_boundaries(hydro.U2);
+  while (t < params.tEnd && nStep < params.nStepmax) {
+    dt = hydro.compute_dt(nStep % 2);
+    if (t + dt > params.tEnd) dt = params.tEnd - t;
+    hydro.godunov_unsplit(nStep, dt);
+    nStep++;
+    t += dt;
+  }
+  ComputeRadialProfileFunctor::apply(hydro, hydro.U);
+  Batch batch(size_t(1) << 30);
+  const int id = batch.admit(params, 0.1);
+  while (batch.run(16) > 0) {
+  }
+  std::vector<double> u = batch.state(id, params);
+  batch.release(id);
+  return argc + (int)u.size() > 0 ? 0 : 1;
+}
+""")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", inc, str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
