@@ -447,7 +447,11 @@ def serve_summary(rates, seconds, max_requests):
         n = max(8, int(rate * seconds))
         solves = workloads.mixed_batch(min(n, max_requests), seed=1, max_side=2048, bubbles=True)
         st = serving.serve(solves, rate, pool_bytes=150 << 30, time_limit_s=seconds * 4)
+        tag = lambda k: f"{k}: {solves[k].kind} {solves[k].params.nx}x{solves[k].params.ny}"
         results.append({"rate_per_s": rate, "requests": len(solves), "completed": st.solves,
+                        "failed_nonfinite": [tag(k) for k in st.failed],
+                        "rerun_fp64_after_nonfinite": [tag(k) for k in st.escalated],
+                        "wasted_cell_updates": st.wasted_cell_updates,
                         "value": st.gcell_per_s, "seconds": st.seconds, **st.percentiles()})
     return results
 

@@ -449,6 +449,16 @@ class Batch:
                                            ctypes.byref(a)), "query")
         return t.value, ns.value, bool(a.value)
 
+    def poll(self, id: int):
+        """(t, nstep, active, ok) of instance id without raising for a
+        stopped solve: ok is False when it hit a non-finite state or a bad dt
+        (query's E2D_ENUMERIC), and t, nstep are where it stopped."""
+        t, ns, a = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
+        rc = self._lib.e2d_batch_query(self._h, int(id), ctypes.byref(t), ctypes.byref(ns), ctypes.byref(a))
+        if rc not in (0, 3):  # E2D_OK, E2D_ENUMERIC
+            self._ck(rc, "query")
+        return t.value, ns.value, bool(a.value), rc == 0
+
     def get_state(self, id: int) -> np.ndarray:
         if id not in self.shapes:
             raise E2DError(1, "get_state", f"instance {id} is not in the batch")  # E2D_EINVAL

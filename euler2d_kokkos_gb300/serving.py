@@ -11,6 +11,14 @@ serve            -- continuous batching under open-loop Poisson arrivals:
                     admitted as slots and pool bytes free up, every admitted
                     solve advances in the same per-iteration launch, and each
                     request's latency (arrival to completion) is recorded.
+
+A FP32C solve whose state turns non-finite is stopped by the batch
+(E2D_ENUMERIC) without affecting the others.  With on_nonfinite="fp64" (the
+default) it is admitted again from its initial state as an FP64 instance --
+the bit-exact FP64 kernels, in the same batch -- and its latency runs from the
+original arrival; "drop" records it in RunStats.failed instead.  FP32 arithmetic
+can break down where FP64 does not: the reference's own single-precision build
+(USE_DOUBLE off) also turns non-finite on such flows.
 """
 from __future__ import annotations
 
@@ -19,7 +27,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import Batch, E2DError, HydroRun
+from . import PRECISION_FP32C, PRECISION_FP64, Batch, E2DError, HydroRun
 
 
 @dataclass
@@ -30,6 +38,9 @@ class RunStats:
     iterations: int = 0
     latencies: list = field(default_factory=list)
     tuning: tuple = ()
+    failed: list = field(default_factory=list)     # indices of solves stopped by a non-finite state
+    escalated: list = field(default_factory=list)  # indices of FP32C solves re-run in FP64
+    wasted_cell_updates: int = 0                   # updates of stopped solves (not in cell_updates)
 
     @property
     def gcell_per_s(self) -> float:
@@ -52,11 +63,53 @@ def _sync_device():
         pass
 
 
-def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, keep=None):
+class _Reaper:
+    """Completion handling shared by run_batched and serve: a solve that
+    reached t_end is done; a stopped one is either queued again in FP64
+    (policy "fp64", FP32C solves only) or recorded as failed."""
+
+    def __init__(self, solves, stats, policy):
+        if policy not in ("fp64", "drop"):
+            raise ValueError("on_nonfinite must be 'fp64' or 'drop'")
+        self.solves, self.stats, self.policy = solves, stats, policy
+        self.fp64 = set()  # indices now running in FP64 after a FP32C failure
+
+    def params(self, k):
+        p = self.solves[k].params
+        if k in self.fp64:
+            p = p.copy()
+            p.precision = PRECISION_FP64
+            p.init()
+        return p
+
+    def reap(self, b, i, k):
+        """State of instance i (solve k): None while it runs; True when it
+        reached t_end; "retry" when it stopped and solve k is to be admitted
+        again in FP64; False when it stopped for good.  Every outcome but
+        None releases the instance."""
+        _, ns, active, ok = b.poll(i)
+        if ok and active:
+            return None
+        b.release(i)
+        if ok:
+            return True
+        p = self.solves[k].params
+        self.stats.wasted_cell_updates += ns * p.nx * p.ny
+        if self.policy == "fp64" and p.precision == PRECISION_FP32C and k not in self.fp64:
+            self.fp64.add(k)
+            self.stats.escalated.append(k)
+            return "retry"
+        self.stats.failed.append(k)
+        return False
+
+
+def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, keep=None,
+                on_nonfinite="fp64"):
     """Advance every solve to its t_end in one batch; solves that do not fit
     wait for room.  keep: optional set of indices whose final states are
-    returned in `states`."""
+    returned in `states`.  on_nonfinite: "fp64" or "drop" (module doc)."""
     stats = RunStats()
+    reaper = _Reaper(solves, stats, on_nonfinite)
     states = {}
     with Batch(riemann="hllc", pool_bytes=pool_bytes, max_instances=max(len(solves), 1)) as b:
         pending = list(range(len(solves)))
@@ -68,7 +121,7 @@ def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, k
             while pending:
                 k = pending[0]
                 try:
-                    live[b.admit(solves[k].params, solves[k].t_end, solves[k].u0)] = k
+                    live[b.admit(reaper.params(k), solves[k].t_end, solves[k].u0)] = k
                 except E2DError as e:
                     if e.status != 2 or not live:
                         raise
@@ -80,15 +133,21 @@ def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, k
             b.run(iters_per_call)
             stats.iterations += iters_per_call
             for i in list(live):
-                t, ns, active = b.query(i)
-                if not active:
-                    k = live.pop(i)
-                    if keep is not None and k in keep:
+                k = live[i]
+                if keep is not None and k in keep:
+                    _, _, active, ok = b.poll(i)
+                    if ok and not active:
                         states[k] = b.get_state(i)
-                    b.release(i)
+                r = reaper.reap(b, i, k)
+                if r is None:
+                    continue
+                live.pop(i)
+                if r == "retry":
+                    pending.insert(0, k)
+                elif r:
                     stats.solves += 1
         stats.seconds = time.perf_counter() - t0
-        stats.cell_updates = b.stats()[0]
+        stats.cell_updates = b.stats()[0] - stats.wasted_cell_updates
         stats.tuning = b.get_tuning()
     return stats, states
 
@@ -117,13 +176,14 @@ def run_one_at_a_time(solves, chunk=256):
 
 
 def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, autotune=True,
-          time_limit_s=None):
+          time_limit_s=None, on_nonfinite="fp64"):
     """Open-loop Poisson arrivals (rate_per_s) of `solves` in order; returns
     RunStats with per-request latencies and the aggregate throughput over
-    the makespan."""
+    the makespan.  on_nonfinite: "fp64" or "drop" (module doc)."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=len(solves)))
     stats = RunStats()
+    reaper = _Reaper(solves, stats, on_nonfinite)
     with Batch(riemann="hllc", pool_bytes=pool_bytes, max_instances=max(len(solves), 1)) as b:
         queue = []          # (index, arrival) waiting for admission
         live = {}           # instance id -> (index, arrival)
@@ -141,7 +201,7 @@ def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, au
             while queue:
                 k, arr = queue[0]
                 try:
-                    i = b.admit(solves[k].params, solves[k].t_end, solves[k].u0)
+                    i = b.admit(reaper.params(k), solves[k].t_end, solves[k].u0)
                 except E2DError as e:
                     if e.status != 2:
                         raise
@@ -160,12 +220,16 @@ def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, au
             stats.iterations += iters_per_call
             done_t = time.perf_counter() - t0
             for i in list(live):
-                _, _, active = b.query(i)
-                if not active:
-                    k, arr = live.pop(i)
+                k, arr = live[i]
+                r = reaper.reap(b, i, k)
+                if r is None:
+                    continue
+                live.pop(i)
+                if r == "retry":
+                    queue.insert(0, (k, arr))
+                elif r:
                     stats.latencies.append(done_t - arr)
-                    b.release(i)
                     stats.solves += 1
         stats.seconds = time.perf_counter() - t0
-        stats.cell_updates = b.stats()[0]
+        stats.cell_updates = b.stats()[0] - stats.wasted_cell_updates
     return stats

@@ -247,3 +247,64 @@ def test_batch_nonfinite_instance_is_isolated(gpu_lib, precision):
         i = alone.admit(good.params, good.t_end, good.u0)
         run_to_end(alone)
         assert np.array_equal(alone.get_state(i), mixed)
+
+
+def test_serving_nonfinite_policies(gpu_lib):
+    """A FP32C solve whose initial state holds a NaN: "drop" records it as
+    failed; "fp64" admits it again as an FP64 instance, which stops too (the
+    NaN is in its input), and then records it.  The other solve completes
+    either way, and the stopped solve's updates are kept out of cell_updates."""
+    from euler2d_kokkos_gb300 import serving
+
+    good, bad = W.mixed_batch(2, seed=51, max_side=128, device_init=False)
+    bad.u0 = bad.u0.copy()
+    bad.u0[0, 10, 10] = np.nan
+    with e2d.Batch(pool_bytes=POOL) as alone:
+        alone.admit(good.params, good.t_end, good.u0)
+        run_to_end(alone)
+        good_updates = alone.stats()[0]
+    for policy in ("drop", "fp64"):
+        st, _ = serving.run_batched([good, bad], pool_bytes=POOL, autotune=False, on_nonfinite=policy)
+        assert st.solves == 1 and st.failed == [1], policy
+        assert st.escalated == ([1] if policy == "fp64" else []), policy
+        assert st.wasted_cell_updates > 0 and st.cell_updates == good_updates, policy
+
+
+# A four-quadrant flow with drawn states (416 x 1824 cells, reflecting walls,
+# split at 0.5) on which FP32 arithmetic breaks down: the FP32C state turns
+# non-finite near t = 0.048 on the column of the vertical split, where the
+# reference's own single-precision build (USE_DOUBLE off) also turns
+# non-finite, near t = 0.05; FP64 runs it to the end.
+BREAKDOWN_T_END = 0.07696256392150672
+BREAKDOWN_STATES = [
+    [1.4045364949998327, 1.2478185891339812, 1.0125626194788715, 1.4112208957238694],
+    [0.5510051598548608, 1.3033349919491264, 1.4899767690701817, 0.8116696708168066],
+    [1.9604589210178323, 0.12702456455098715, -1.1540322213586327, -0.050099086017271144],
+    [1.3025418760856602, 1.7962252840716093, 0.2289799732296557, -1.1532139468078726],
+]
+
+
+def test_fp32_breakdown_is_rerun_in_fp64(gpu_lib):
+    """run_batched stops the FP32C solve of the flow above with
+    E2D_ENUMERIC, runs it again in FP64 and returns the FP64 path's state bit
+    for bit."""
+    from euler2d_kokkos_gb300 import serving
+
+    p = e2d.make_params(416, 1824, problem="four_quadrant", riemann="hllc", gamma0=1.4, cfl=0.8,
+                        bc=(2, 2, 2, 2), precision=e2d.PRECISION_FP32C)
+    p.fq_split_x = p.fq_split_y = 0.5
+    for q in range(4):
+        for v in range(4):
+            p.fq_state[q][v] = BREAKDOWN_STATES[q][v]
+    s = W.Solve("four_quadrant", p, None, BREAKDOWN_T_END)
+    st, states = serving.run_batched([s], pool_bytes=POOL, autotune=False, keep={0})
+    assert st.escalated == [0] and st.failed == [] and st.solves == 1
+    p64 = p.copy()
+    p64.precision = e2d.PRECISION_FP64
+    with e2d.HydroRun(p64.init()) as h:
+        t, ns = 0.0, 0
+        while t < BREAKDOWN_T_END:
+            prev = ns
+            t, ns, _ = h.step_n(256, BREAKDOWN_T_END, t, ns, want_trace=False)
+            assert ns > prev
+        assert np.array_equal(h.current(ns), states[0])
