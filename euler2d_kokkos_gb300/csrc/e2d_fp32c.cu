@@ -57,12 +57,13 @@ __device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
 
 // Constants broadcast to both halves of a float2.
 struct C2 {
-  float2 half, smallr, smallp, smallc2, gamma0, gm1, entho, st;
+  float2 half, mhalf, smallr, smallp, smallc2, gamma0, gm1, entho, st;
 };
 
 __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
   C2 k;
   k.half = f2(0.5f);
+  k.mhalf = f2(-0.5f);
   k.smallr = f2(ph.smallr);
   k.smallp = f2(ph.smallp);
   k.smallc2 = f2(ph.smallc2);
@@ -79,29 +80,40 @@ __device__ __forceinline__ void prims2(const C2 &k, float2 rho, float2 e, float2
   const float2 d = max2(rho, k.smallr);
   const float2 inv = rcp2(d);
   const float2 u = mx * inv, v = my * inv;
-  const float2 eken = k.half * fma2(u, u, v * v);
-  const float2 ei = fma2(e, inv, neg2(eken));
+  const float2 ei = fma2(e, inv, k.mhalf * fma2(u, u, v * v));  // e/d - (u^2+v^2)/2
   q[E2D_ID] = d;
   q[E2D_IP] = max2(k.gm1 * d * ei, d * k.smallp);
   q[E2D_IU] = u;
   q[E2D_IV] = v;
 }
 
+// Three-input minimum and maximum (one instruction each on sm_100 and later).
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 // slope_unsplit_hydro_2d_scalar (src/HydroBaseFunctor.h:421-455), one
 // direction, two cells; slope_type 0 is handled by the caller.  The
 // reference's form -- zero when (q-qm)*(qp-q) <= 0, else
-// sign(dcen) * min(st|q-qm|, st|qp-q|, |dcen|) -- is evaluated as
-// s * max(0, min(st * min(s*(q-qm), s*(qp-q)), |dcen|)) with s = sign(dcen):
-// both one-sided differences share the sign of dcen exactly when their
-// product is positive, and a difference of the other sign makes the inner
-// minimum negative.
+// sign(dcen) * min(st|q-qm|, st|qp-q|, |dcen|) -- is the minmod of the three
+// differences a = st(q-qm), b = st(qp-q), c = dcen:
+// max(0, min(a,b,c)) + min(0, max(a,b,c)).  When a and b have one sign, c
+// (half their sum) has it too and the minmod is the one of smallest
+// magnitude; when they differ both terms are 0.
+__device__ __forceinline__ float2 minmod2(float2 a, float2 b, float2 c) {
+  const float2 lo = make_float2(min3f(a.x, b.x, c.x), min3f(a.y, b.y, c.y));
+  const float2 hi = make_float2(max3f(a.x, b.x, c.x), max3f(a.y, b.y, c.y));
+  return max2(lo, f2(0.0f)) + min2(hi, f2(0.0f));
+}
 __device__ __forceinline__ float2 slope2(const C2 &k, float2 q, float2 qp, float2 qm) {
-  const float2 dl = q - qm;
-  const float2 dr = qp - q;
-  const float2 dcen = k.half * (qp - qm);
-  const float2 s = make_float2(copysignf(1.0f, dcen.x), copysignf(1.0f, dcen.y));
-  const float2 lim = k.st * min2(s * dl, s * dr);
-  return s * max2(min2(lim, abs2(dcen)), f2(0.0f));
+  return minmod2(k.st * (q - qm), k.st * (qp - q), k.half * (qp - qm));
 }
 
 // riemann_hllc (src/HydroBaseFunctor.h:704-809) for two faces.
@@ -128,16 +140,20 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
   const float2 sdu = S - us;
   const float2 isds = rcp2(S - ustar);
   const float2 rstar = rs * sdu * isds;
-  const float2 etotstar = fma2(ptotstar, ustar, fma2(sdu, es, neg2(ps * us))) * isds;
-  // SL > 0: left state; else star (left or right); SR <= 0: right state.
-  // (no branch around the selects: the x and y solves of a row stay in one
-  // basic block)
-  const bool sx = SL.x > 0.0f, sy = SL.y > 0.0f;
-  const bool tx = !sx && (lx || SR.x > 0.0f), ty = !sy && (ly || SR.y > 0.0f);
-  const float2 ro = sel2(sx, sy, rl, sel2(tx, ty, rstar, rr));
-  const float2 uo = sel2(sx, sy, ul, sel2(tx, ty, ustar, ur));
-  const float2 po = sel2(sx, sy, pl, sel2(tx, ty, ptotstar, pr));
-  const float2 eo = sel2(sx, sy, etotl, sel2(tx, ty, etotstar, etotr));
+  const float2 etotstar = fma2(ptotstar, ustar, fma2(sdu, es, (ps * us) * f2(-1.0f))) * isds;
+  // The reference samples: SL > 0: left state; else ustar > 0: left star;
+  // else SR > 0: right star; else right state.  SL > 0 implies ustar > 0
+  // (then rcl*ul > gamma*pl and rcr*ur > gamma*pr, so the numerator of ustar
+  // exceeds (gamma+1)*pl + (gamma-1)*pr > 0), and SR <= 0 implies
+  // ustar <= 0, so the choice is: the side's own state when its outer wave
+  // S is on the far side of x/t = 0 ((S > 0) == (ustar > 0)), else its star
+  // state.  (No branch around the selects: the x and y solves of a row stay
+  // in one basic block.)
+  const bool ox = (S.x > 0.0f) == lx, oy = (S.y > 0.0f) == ly;
+  const float2 ro = sel2(ox, oy, rs, rstar);
+  const float2 uo = sel2(ox, oy, us, ustar);
+  const float2 po = sel2(ox, oy, ps, ptotstar);
+  const float2 eo = sel2(ox, oy, es, etotstar);
   f[E2D_ID] = ro * uo;
   f[E2D_IU] = fma2(f[E2D_ID], uo, po);
   f[E2D_IP] = (eo + po) * uo;
@@ -493,6 +509,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
   const C2 k = make_c2(ph);
   const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
   const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
+  const float2 hdtdx = k.mhalf * dtdx, hdtdy = k.mhalf * dtdy;  // exact halvings
 
   float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
   float2 ymax_prev[4];  // YMAX states of row m-1
@@ -595,36 +612,40 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
         dqy[v] = slope2(k, qb[v], qc[v], qa[v]);
       }
     }
-    // trace sources (src/HydroBaseFunctor.h:246-249)
-    float2 s0[4];
+    // trace sources (src/HydroBaseFunctor.h:246-249), negated: ns0 = -s0,
+    // and the half-step terms below take -1/2 (exact: the sign is the only
+    // difference)
+    float2 ns0[4];
     {
       const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
       const float2 div = dqx[E2D_IU] + dqy[E2D_IV];
       const float2 ir = rcp2(r);
-      s0[E2D_ID] = neg2(fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r)));
-      s0[E2D_IP] = neg2(fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p)));
-      s0[E2D_IU] = neg2(fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir)));
-      s0[E2D_IV] = neg2(fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir)));
+      ns0[E2D_ID] = fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r));
+      ns0[E2D_IP] = fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p));
+      ns0[E2D_IU] = fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir));
+      ns0[E2D_IV] = fma2(u, dqx[E2D_IV], fma2(v, dqy[E2D_IV], dqy[E2D_IP] * ir));
     }
-    // x faces of row m (fluxes needed for rows rb..re-1) and y faces of row
-    // m (the flux of face (m-1|m) from the saved YMAX of row m-1, needed for
-    // m >= rb).  Both Riemann solves run on every row, their results masked
-    // outside those rows: the loop body has no branch around them, so the
-    // two independent solves can be scheduled together.
+    // x faces of row m and y faces of row m (the flux of face (m-1|m) from
+    // the saved YMAX of row m-1).  Both Riemann solves run on every row:
+    // the loop body has no branch around them, so the two independent
+    // solves can be scheduled together.  The update of row m-1 (m >= rb+1)
+    // reads the x-fluxes of row m-1 and the y-fluxes of iterations m-1 and
+    // m, so the solves of iteration rb-1 (and the x-solve of row re) are
+    // never read.
     float2 xl[4], xr[4], ymin[4], ymax[4];
+    // q -/+ dq/2 as one FMA each (the halving is exact), the source term
+    // as ns0 * (-dt/(2dx)): the same values as (q -/+ dq*0.5) + s0*0.5*dt/dx
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const float2 hx = k.half * dqx[v];
-      const float2 sx_ = k.half * s0[v] * dtdx;
-      float2 xmin = (qb[v] - hx) + sx_;
-      float2 xmax = (qb[v] + hx) + sx_;
+      const float2 sx_ = ns0[v] * hdtdx;
+      float2 xmin = fma2(dqx[v], k.mhalf, qb[v]) + sx_;
+      float2 xmax = fma2(dqx[v], k.half, qb[v]) + sx_;
       if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
       xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
       xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
-      const float2 hy = k.half * dqy[v];
-      const float2 sy_ = k.half * s0[v] * dtdy;
-      ymin[v] = (qb[v] - hy) + sy_;
-      ymax[v] = (qb[v] + hy) + sy_;
+      const float2 sy_ = ns0[v] * hdtdy;
+      ymin[v] = fma2(dqy[v], k.mhalf, qb[v]) + sy_;
+      ymax[v] = fma2(dqy[v], k.half, qb[v]) + sy_;
     }
     ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
     ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
@@ -636,13 +657,12 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       float2 f[4];
       riemann2<RS>(ph, k, xl, xr, fx);
       riemann2<RS>(ph, k, yl, yr, f);
-      const bool xrow = (m >= rb) && (m < re), yrow = m >= rb;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) fx[v] = xrow ? fx[v] * dtdx : f2(0.0f);
-      fy[E2D_ID] = yrow ? f[E2D_ID] * dtdy : f2(0.0f);
-      fy[E2D_IP] = yrow ? f[E2D_IP] * dtdy : f2(0.0f);
-      fy[E2D_IU] = yrow ? f[E2D_IV] * dtdy : f2(0.0f);
-      fy[E2D_IV] = yrow ? f[E2D_IU] * dtdy : f2(0.0f);
+      for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
+      fy[E2D_ID] = f[E2D_ID] * dtdy;
+      fy[E2D_IP] = f[E2D_IP] * dtdy;
+      fy[E2D_IU] = f[E2D_IV] * dtdy;
+      fy[E2D_IV] = f[E2D_IU] * dtdy;
     }
     // compensated update of row m-1
     if (m >= rb + 1) {
