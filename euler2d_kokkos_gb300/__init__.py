@@ -452,10 +452,11 @@ class Batch:
     def poll(self, id: int):
         """(t, nstep, active, ok) of instance id without raising for a
         stopped solve: ok is False when it hit a non-finite state or a bad dt
-        (query's E2D_ENUMERIC), and t, nstep are where it stopped."""
+        (query's E2D_ENUMERIC) or a device wait of its step gave up
+        (E2D_ETIMEOUT), and t, nstep are where it stopped."""
         t, ns, a = ctypes.c_double(), ctypes.c_int(), ctypes.c_int()
         rc = self._lib.e2d_batch_query(self._h, int(id), ctypes.byref(t), ctypes.byref(ns), ctypes.byref(a))
-        if rc not in (0, 3):  # E2D_OK, E2D_ENUMERIC
+        if rc not in (0, 3, 4):  # E2D_OK, E2D_ENUMERIC, E2D_ETIMEOUT
             self._ck(rc, "query")
         return t.value, ns.value, bool(a.value), rc == 0
 

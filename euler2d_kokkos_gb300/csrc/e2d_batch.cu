@@ -443,6 +443,8 @@ int e2d_batch_admit(e2d_batch *b, const e2d_params *pin, double t_end, const dou
   }
   if (launch_f32c_from_f64(kp, stage, w0, b->stream) != cudaSuccess) return undo(E2D_ECUDA, "admit: convert");
   BatchInst I{};
+  if (!encode_f32c_map(&I.tm[0], w0, kp) || !encode_f32c_map(&I.tm[1], w1, kp))
+    return undo(E2D_ECUDA, "admit: TMA map");
   I.kp = kp;
   I.w[0] = w0;
   I.w[1] = w1;
@@ -495,6 +497,7 @@ int e2d_batch_query(e2d_batch *b, int id, double *t, int *nstep, int *active) {
   if (t) *t = m.t();
   if (nstep) *nstep = m.nstep();
   if (active) *active = m.active();
+  if (m.status() & E2D_FLAG_TIMEOUT) return berr(b, E2D_ETIMEOUT, "instance stopped: a row-staging wait gave up");
   if (m.status() & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT)) return berr(b, E2D_ENUMERIC, "instance hit NaN/Inf or a bad dt");
   return E2D_OK;
 }

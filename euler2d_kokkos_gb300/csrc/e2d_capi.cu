@@ -24,6 +24,7 @@ struct e2d_sim {
   double *U[2] = {nullptr, nullptr};  // FP64: U and U2 of the reference
   double *Q = nullptr;                // FP64: primitives scratch (one full array)
   float *W[2] = {nullptr, nullptr};   // FP32C: compensated U and U2 (8 float planes)
+  CUtensorMap TM[2];                  // FP32C: TMA maps of W[0], W[1] (row staging)
   double *stage = nullptr;            // FP32C: FP64 staging array (set/get/init)
   double *partial = nullptr;          // reduction partials
   double *red_out = nullptr;          // reduction results (device)
@@ -124,7 +125,7 @@ const char *riemann_name(int r) {
 // Kernels of one step of the device time loop, input buffer `par`.
 cudaError_t enqueue_step(e2d_sim *s, int par) {
   if (s->fp32)
-    return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1,
+    return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 1,
                             0.0, s->stream);
   double *in = s->U[par], *out = s->U[par ^ 1];
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK;
@@ -279,6 +280,7 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
     for (int k = 0; k < 2; ++k) {
       if (cudaMalloc(&s->W[k], sizeof(float) * wn) != cudaSuccess) return fail(E2D_ENOMEM);
       if (cudaMemsetAsync(s->W[k], 0, sizeof(float) * wn, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+      if (!encode_f32c_map(&s->TM[k], s->W[k], s->kp32)) return fail(E2D_ECUDA);
     }
     if (cudaMalloc(&s->stage, sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
   } else {
@@ -458,7 +460,7 @@ int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   if (!s) return E2D_EINVAL;
   const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
   if (s->fp32) {
-    E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 0, dt,
+    E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 0, dt,
                                s->stream), "godunov step");
     return E2D_OK;
   }
@@ -497,7 +499,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
       if (!a || !b || !c2) return set_err(s, E2D_ECUDA, "event create");
       if (s->fp32) {
         E2D_CK(s, cudaEventRecord(a, s->stream), "event");
-        E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->clk, 1, 0.0,
+        E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 1, 0.0,
                                    s->stream), "step");
         E2D_CK(s, cudaEventRecord(b, s->stream), "event");
         marks.push_back({"k_step_f32c<" + rs + ">", {a, b}});
@@ -539,6 +541,8 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
     E2D_CK(s, cudaMemcpy(dt_trace, s->dt_trace, sizeof(double) * taken, cudaMemcpyDeviceToHost), "trace copy");
   *t = s->clk_host->t;
   *nStep = s->clk_host->nstep;
+  if (s->clk_host->status & E2D_FLAG_TIMEOUT)
+    return set_err(s, E2D_ETIMEOUT, "a row-staging wait gave up: the state of this call is incomplete");
   if (s->clk_host->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT))
     return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
                                                                               : "non-positive or non-finite dt");

@@ -18,7 +18,8 @@
 // no block barrier is taken in the march.  Input rows reach the warp either
 // as register loads one row ahead or (default variants) through a per-warp
 // shared-memory ring filled by cp.async two rows ahead, ordered by one warp
-// barrier per row.  The two columns of a lane are computed together with
+// barrier per row; variant 6 fills the ring of interior strips by TMA copies
+// (one per row) waited on with mbarriers, each wait bounded.  The two columns of a lane are computed together with
 // Blackwell's packed FP32 instructions (FFMA2 / FADD2 / FMUL2 on float2).
 // Ghost cells are read through the boundary map, so no fill pass runs and
 // ghost cells of the arrays are never read.  Algorithmic traffic: 32 B read
@@ -26,6 +27,10 @@
 #include "e2d_common.cuh"
 #include "e2d_internal.h"
 
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstdlib>
 #include <type_traits>
 
 namespace e2d {
@@ -428,7 +433,10 @@ __device__ __forceinline__ void load_row(const KParams32 &kp, const float *__res
 // planes (hi, lo) x 64 columns of one row, each lane copying and later
 // reading only its own two columns.  PFD = 0: rows loaded to registers.
 constexpr int SLOT = 8 * 64;  // floats per slot
-constexpr size_t ring_bytes(int pfd) { return pfd > 0 ? sizeof(float) * WPB * (pfd + 3) * SLOT : 0; }
+constexpr int kMaxSlots = 8;  // ring slots (PFD + 3) a warp may have
+// (+128 bytes: the ring starts at the first 128-byte boundary of the
+// dynamic shared memory, the alignment a tiled TMA destination needs)
+constexpr size_t ring_bytes(int pfd) { return pfd > 0 ? sizeof(float) * WPB * (pfd + 3) * SLOT + 128 : 0; }
 
 __device__ __forceinline__ void cp_async16(float *dst, const float *src) {
   const unsigned int d = (unsigned int)__cvta_generic_to_shared(dst);
@@ -441,6 +449,67 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// TMA row staging (interior strips of the staged variants): one
+// cp.async.bulk.tensor per row and warp copies the 8 planes x 64 columns of
+// a row (a box of 64 x 1 x 8 of the state's tensor map) into a ring slot,
+// completing on the slot's mbarrier.  The box starts at a column multiple
+// of 4 (x * 4 bytes a multiple of 16, as a tiled copy requires).  Each warp
+// owns one mbarrier per ring slot; bit s of `phase` is the parity of slot
+// s's next completion.
+constexpr unsigned int kRowBytes = 8u * 64u * sizeof(float);
+constexpr unsigned long long kWaitNs = 1000000000ull;  // bounded waits give up after 1 s
+
+__device__ __forceinline__ unsigned int smem_u32(const void *p) { return (unsigned int)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long *bar, unsigned int bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned int parity) {
+  unsigned int ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits (every lane) for the completion of phase `parity` of *bar; false,
+// for the whole warp, once kWaitNs have passed without it.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned int parity) {
+  bool ok = mbar_try_wait(bar, parity);
+  if (!__all_sync(0xffffffffu, ok)) {
+    const unsigned long long t0 = global_ns();
+    while (!ok && global_ns() - t0 < kWaitNs) ok = mbar_try_wait(bar, parity);
+    ok = __all_sync(0xffffffffu, ok);
+  }
+  return ok;
+}
+
+// The warp's ring barriers: initialised once per kernel, before any copy.
+__device__ __forceinline__ void ring_bars_init(unsigned long long *bars, int nslots, int lane) {
+  if (lane < nslots) mbar_init(bars + lane, 1u);
+  mbar_init_fence();
+  __syncwarp();
+}
 
 // Source row of array row r: itself, or through the boundary map when the
 // strip touches a ghost row (`yghost`, warp-uniform); fv: negate IV.
@@ -475,6 +544,21 @@ __device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__re
   }
 }
 
+// Copies array row r into a ring slot with one TMA copy (interior strips):
+// lane 0 arms the slot's barrier for the row's bytes and issues the copy.
+// The caller has passed a __syncwarp after every lane's last read of the
+// slot; the proxy fence orders those reads before the copy engine's writes.
+__device__ __forceinline__ void stage_row_tma(const KGeom &g, const CUtensorMap *map, int r, int cs, int lane,
+                                              bool yghost, float *slot, unsigned long long *bar) {
+  bool fv;
+  const int sr = source_row(g, r, yghost, fv);
+  fence_proxy_async_smem();
+  if (lane == 0) {
+    mbar_arrive_expect(bar, kRowBytes);
+    tma_load_3d(slot, map, cs, sr, 0, bar);
+  }
+}
+
 // One warp marches strip (sx, sy) of an instance: rows rb-2 .. re+1 are
 // read, rows rb .. re-1 written.  With a target, the CFL term of the new
 // state is folded into *target once per fold unit -- the strip's 60 output
@@ -483,12 +567,13 @@ __device__ __forceinline__ void stage_row(const KParams32 &kp, const float *__re
 // kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
-template <int RS, int PFD>
+template <int RS, int PFD, int TMA>
 __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
-                                            unsigned int *status, float *ring) {
+                                            unsigned int *status, float *ring, const CUtensorMap *map,
+                                            unsigned long long *bars, unsigned int &phase) {
   // sum of the lane's new conserved values over the strip: NaN or infinite
   // when one of them is (a sum that overflows FP32 reads as non-finite too)
   float2 nfacc = f2(0.0f);
@@ -541,15 +626,50 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     source_row(g, r, yghost, fv);
     if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
   };
+  // Staged variants: interior strips (`bulk`) fill the ring by TMA copies
+  // and wait on the slots' barriers; boundary strips copy each lane's
+  // boundary-mapped columns by cp.async and wait on commit groups.
+  const bool bulk = (TMA != 0) && (PFD > 0) && direct;
+  unsigned int pending = 0u;  // slots with a TMA copy not yet waited for
+  auto stage = [&](int r, int sl) {
+    if (bulk) {
+      // wait_test: the first row of strip (1, 0) is never copied
+      if (kp.wait_test && sx == 1 && sy == 0 && r == rb - 2) return;
+      stage_row_tma(g, map, r, cb - 2, lane, yghost, slot_of(sl), bars + sl);
+      pending |= 1u << sl;
+    } else {
+      stage_row(kp, w_in, r, cb - 2, lane, direct, yghost, s0, s1, slot_of(sl));
+    }
+  };
+  auto wait_slot = [&](int sl) {
+    const bool done = mbar_wait(bars + sl, (phase >> sl) & 1u);
+    if (done) phase ^= 1u << sl, pending &= ~(1u << sl);
+    return done;
+  };
+  // a wait that ran out: flag it, let the copies in flight land (bounded
+  // too) before the ring is reused or the block exits, leave the strip
+  auto give_up = [&]() {
+    if (lane == 0) atomicOr(status, (unsigned)E2D_FLAG_TIMEOUT);
+    for (int sl = 0; sl < R; ++sl)
+      if (pending & (1u << sl)) wait_slot(sl);
+  };
   if ((PFD > 0)) {
-    // rows rb-2 .. rb+PFD-1 into slots 0 .. PFD+1, one commit group each,
-    // after every lane is done with the ring's previous strip
+    // rows rb-2 .. rb+PFD-1 into slots 0 .. PFD+1 (one commit group each on
+    // the cp.async path), after every lane is done with the ring's previous
+    // strip
     __syncwarp();
     for (int r = rb - 2; r < rb + PFD; ++r) {
-      stage_row(kp, w_in, r, cb - 2, lane, direct, yghost, s0, s1, slot_of(r - rb + 2));
-      cp_async_commit();
+      stage(r, r - rb + 2);
+      if (!bulk) cp_async_commit();
     }
-    cp_async_wait<(PFD > 0 ? PFD : 0)>();
+    if (bulk) {
+      if (!(wait_slot(0) && wait_slot(1))) {
+        give_up();
+        return;
+      }
+    } else {
+      cp_async_wait<(PFD > 0 ? PFD : 0)>();
+    }
     __syncwarp();  // lanes read columns other lanes copied
     float2 u[4];
     staged_hi(rb - 2, 0, u);
@@ -573,11 +693,18 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       // barrier makes every lane's copies visible to the warp and orders
       // every lane's reads of row m-2 (previous iteration) before the copy
       // of row m+1+PFD into that slot
-      cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
+      if (bulk) {
+        if (!wait_slot(wrap(sm1 + 2))) {
+          give_up();
+          return;
+        }
+      } else {
+        cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
+      }
       __syncwarp();
       const int rn = m + 1 + PFD;
-      if (rn <= re + 1) stage_row(kp, w_in, rn, cb - 2, lane, direct, yghost, s0, s1, slot_of(wrap(sm1 + R - 1)));
-      cp_async_commit();
+      if (rn <= re + 1) stage(rn, wrap(sm1 + R - 1));
+      if (!bulk) cp_async_commit();
       float2 u[4];
       staged_hi(m + 1, wrap(sm1 + 2), u);
       prims2(k, u[0], u[1], u[2], u[3], qc);
@@ -747,10 +874,20 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
 
 extern __shared__ __align__(16) float g_ring[];
 
-template <int RS, int MINB, int PFD>
+// The warp's row ring: g_ring rounded up to 128 bytes (ring_bytes reserves
+// the slack), then PFD + 3 slots of 2 KB per warp, so every slot is 128-byte
+// aligned.
+template <int PFD>
+__device__ __forceinline__ float *warp_ring(int warp) {
+  const unsigned int a = smem_u32(g_ring);
+  return g_ring + ((128u - (a & 127u)) & 127u) / sizeof(float) + warp * (PFD + 3) * SLOT;
+}
+
+template <int RS, int MINB, int PFD, int TMA>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f32c(const KParams32 kp, const float *__restrict__ w_in, float *__restrict__ w_out,
-                DevClock *clk, const int use_clock, const double host_dt) {
+                const __grid_constant__ CUtensorMap tm_in, DevClock *clk, const int use_clock,
+                const double host_dt) {
   const KGeom &g = kp.g;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
@@ -758,6 +895,7 @@ __global__ void __launch_bounds__(NT, MINB)
   // dt of this step (FP64, src/main.cpp:128-134) by one thread per block
   __shared__ double s_dt[3];
   __shared__ int s_run, s_slot;
+  __shared__ unsigned long long s_bars[TMA ? WPB * kMaxSlots : 1];  // ring slot barriers, per warp
   if (tid == 0) {
     double dt = host_dt;
     int run = 1, slot = 0;
@@ -786,10 +924,14 @@ __global__ void __launch_bounds__(NT, MINB)
   const int SH = kp.strip_h;
   const int nsy = (g.ny + SH - 1) / SH;
   const int strip = blockIdx.x * WPB + (tid >> 5);
-  if (strip < nsx * nsy)
-    march_strip<RS, PFD>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
+  unsigned long long *bars = s_bars + (TMA ? (tid >> 5) * kMaxSlots : 0);
+  unsigned int phase = 0u;
+  if (strip < nsx * nsy) {
+    if (TMA && PFD > 0) ring_bars_init(bars, PFD + 3, lane);
+    march_strip<RS, PFD, TMA>(kp, w_in, w_out, dtdx, dtdy, strip % nsx, strip / nsx, lane,
                          use_clock ? &clk->acc[slot ^ 1] : nullptr, &clk->status,
-                         g_ring + (tid >> 5) * (PFD + 3) * SLOT);
+                         warp_ring<PFD>(tid >> 5), &tm_in, bars, phase);
+  }
   if (!use_clock) return;
 
   // the last block to finish advances the loop state (src/main.cpp:139-143)
@@ -833,7 +975,7 @@ __device__ __forceinline__ void batch_finalize(BatchInst &I) {
   I.dt = dtn;
   I.dtdx = (float)(dtn / I.kp.ph64.dx);
   I.dtdy = (float)(dtn / I.kp.ph64.dy);
-  I.active = (t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
+  I.active = (t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT | E2D_FLAG_TIMEOUT));
   I.done = 0u;
 }
 
@@ -842,12 +984,16 @@ __device__ __forceinline__ void batch_finalize(BatchInst &I) {
 // instance's own dt, folds the instance's next CFL maximum, and the last
 // strip of each instance advances that instance's loop state.  Results of an
 // instance do not depend on the other instances in the batch.
-template <int RS, int MINB, int PFD>
+template <int RS, int MINB, int PFD, int TMA>
 __global__ void __launch_bounds__(NT, MINB)
     k_batch_f32c(BatchInst *__restrict__ insts, const int *__restrict__ list_slots,
                  const int *__restrict__ strip_begin, const int n_inst, const int total_strips) {
   const int lane = threadIdx.x & 31;
   const int nwarps = gridDim.x * WPB;
+  __shared__ unsigned long long s_bars[TMA ? WPB * kMaxSlots : 1];  // ring slot barriers, per warp
+  unsigned long long *bars = s_bars + (TMA ? (threadIdx.x >> 5) * kMaxSlots : 0);
+  unsigned int phase = 0u;  // carried across the warp's strips
+  if (TMA && PFD > 0) ring_bars_init(bars, PFD + 3, lane);
   for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < total_strips; w += nwarps) {
     // instance k with strip_begin[k] <= w < strip_begin[k + 1]
     int lo = 0, hi = n_inst;
@@ -863,9 +1009,9 @@ __global__ void __launch_bounds__(NT, MINB)
     const KParams32 &kp = I.kp;
     const int par = I.par;
     const int strip = w - strip_begin[lo];
-    march_strip<RS, PFD>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
+    march_strip<RS, PFD, TMA>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
                          strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
-                         g_ring + (threadIdx.x >> 5) * (PFD + 3) * SLOT);
+                         warp_ring<PFD>(threadIdx.x >> 5), &I.tm[par], bars, phase);
     if (lane == 0) {
       __threadfence();
       const unsigned int ticket = atomicAdd(&I.done, 1u);
@@ -886,7 +1032,7 @@ __global__ void k_batch_arm(BatchInst *I) {
   I->dt = dt;
   I->dtdx = (float)(dt / I->kp.ph64.dx);
   I->dtdy = (float)(dt / I->kp.ph64.dy);
-  I->active = (I->t < I->t_end) && !(I->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
+  I->active = (I->t < I->t_end) && !(I->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT | E2D_FLAG_TIMEOUT));
   I->done = 0u;
 }
 
@@ -902,30 +1048,33 @@ int strips_of(const KParams32 &kp) {
 template <class F>
 static void with_variant(int v, F &&f) {
   using std::integral_constant;
+  using I0 = integral_constant<int, 0>;
+  using I1 = integral_constant<int, 1>;
   switch (v) {
-    case 0: f(integral_constant<int, 1>{}, integral_constant<int, 0>{}); break;
-    case 2: f(integral_constant<int, 3>{}, integral_constant<int, 0>{}); break;
-    case 3: f(integral_constant<int, 2>{}, integral_constant<int, 0>{}); break;
-    case 4: f(integral_constant<int, 3>{}, integral_constant<int, 2>{}); break;
-    case 5: f(integral_constant<int, 4>{}, integral_constant<int, 2>{}); break;
-    default: f(integral_constant<int, 4>{}, integral_constant<int, 0>{}); break;
+    case 0: f(integral_constant<int, 1>{}, I0{}, I0{}); break;
+    case 2: f(integral_constant<int, 3>{}, I0{}, I0{}); break;
+    case 3: f(integral_constant<int, 2>{}, I0{}, I0{}); break;
+    case 4: f(integral_constant<int, 3>{}, integral_constant<int, 2>{}, I0{}); break;
+    case 5: f(integral_constant<int, 4>{}, integral_constant<int, 2>{}, I0{}); break;
+    case 6: f(integral_constant<int, 4>{}, integral_constant<int, 2>{}, I1{}); break;
+    default: f(integral_constant<int, 4>{}, I0{}, I0{}); break;
   }
 }
-static_assert(kF32cVariants == 6, "with_variant covers variants 0..5");
+static_assert(kF32cVariants == 7, "with_variant covers variants 0..6");
 
-template <int MINB, int PFD>
+template <int MINB, int PFD, int TMA>
 static void launch_batch_v(int riemann, BatchInst *insts, const int *slots, const int *sb, int n, int total,
                            int grid, cudaStream_t s) {
   const size_t sm = ring_bytes(PFD);
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_batch_f32c<E2D_RIEMANN_HLLC, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLLC, MINB, PFD, TMA><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
     case E2D_RIEMANN_HLL:
-      k_batch_f32c<E2D_RIEMANN_HLL, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_HLL, MINB, PFD, TMA><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
     default:
-      k_batch_f32c<E2D_RIEMANN_APPROX, MINB, PFD><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
+      k_batch_f32c<E2D_RIEMANN_APPROX, MINB, PFD, TMA><<<grid, NT, sm, s>>>(insts, slots, sb, n, total);
       break;
   }
 }
@@ -934,8 +1083,8 @@ cudaError_t launch_batch_f32c(int riemann, int variant, BatchInst *insts, const 
                               const int *strip_begin, int n_inst, int total_strips, int grid_blocks,
                               cudaStream_t s) {
   if (n_inst <= 0 || total_strips <= 0) return cudaSuccess;
-  with_variant(variant, [&](auto minb, auto pfd) {
-    launch_batch_v<decltype(minb)::value, decltype(pfd)::value>(riemann, insts, list_slots, strip_begin, n_inst,
+  with_variant(variant, [&](auto minb, auto pfd, auto tma) {
+    launch_batch_v<decltype(minb)::value, decltype(pfd)::value, decltype(tma)::value>(riemann, insts, list_slots, strip_begin, n_inst,
                                                                 total_strips, grid_blocks, s);
   });
   return cudaGetLastError();
@@ -950,9 +1099,9 @@ template <int RS>
 static int batch_occupancy(int variant) {
   int n = 0;
   cudaError_t e = cudaErrorInvalidValue;
-  with_variant(variant, [&](auto minb, auto pfd) {
-    constexpr int M = decltype(minb)::value, P = decltype(pfd)::value;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, M, P>, NT, ring_bytes(P));
+  with_variant(variant, [&](auto minb, auto pfd, auto tma) {
+    constexpr int M = decltype(minb)::value, P = decltype(pfd)::value, T = decltype(tma)::value;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_batch_f32c<RS, M, P, T>, NT, ring_bytes(P));
   });
   return (e == cudaSuccess && n > 0) ? n : 1;
 }
@@ -991,6 +1140,8 @@ void make_kparams32(const e2d_params &p, KParams32 *kp) {
   kp->wplane = (long long)kp->wpitch * p.jsize;
   kp->variant = 4;  // 3 blocks per SM, rows staged by cp.async (fastest at 8192^2)
   kp->strip_h = default_strip_h(p.nx, p.ny);
+  const char *wt = std::getenv("E2D_TEST_WAIT_TIMEOUT");
+  kp->wait_test = (wt && std::atoi(wt) != 0) ? 1 : 0;
 }
 
 // Dynamic plus static shared memory above 48 KB must be enabled per kernel
@@ -999,12 +1150,12 @@ template <int RS>
 static cudaError_t configure_rs() {
   cudaError_t e = cudaSuccess;
   for (int v = 0; v < kF32cVariants && e == cudaSuccess; ++v)
-    with_variant(v, [&](auto minb, auto pfd) {
-      constexpr int M = decltype(minb)::value, P = decltype(pfd)::value;
+    with_variant(v, [&](auto minb, auto pfd, auto tma) {
+      constexpr int M = decltype(minb)::value, P = decltype(pfd)::value, T = decltype(tma)::value;
       if (P > 0) {  // the kernels' static shared memory comes on top of the ring
-        e = cudaFuncSetAttribute(k_step_f32c<RS, M, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_bytes(P));
+        e = cudaFuncSetAttribute(k_step_f32c<RS, M, P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_bytes(P));
         if (e == cudaSuccess)
-          e = cudaFuncSetAttribute(k_batch_f32c<RS, M, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+          e = cudaFuncSetAttribute(k_batch_f32c<RS, M, P, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)ring_bytes(P));
       }
     });
@@ -1045,33 +1196,59 @@ cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, i
   return launch_f32c_dt_to(kp, w, slot < 0 ? &clk->invdt_bits : &clk->acc[slot], &clk->status, s);
 }
 
-template <int MINB, int PFD>
+template <int MINB, int PFD, int TMA>
 static void launch_step_v(const KParams32 &kp, int riemann, int blocks, const float *w_in, float *w_out,
-                          DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
+                          const CUtensorMap &tm, DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
   const size_t sm = ring_bytes(PFD);
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_step_f32c<E2D_RIEMANN_HLLC, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLLC, MINB, PFD, TMA><<<blocks, NT, sm, s>>>(kp, w_in, w_out, tm, clk, use_clock, host_dt);
       break;
     case E2D_RIEMANN_HLL:
-      k_step_f32c<E2D_RIEMANN_HLL, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_HLL, MINB, PFD, TMA><<<blocks, NT, sm, s>>>(kp, w_in, w_out, tm, clk, use_clock, host_dt);
       break;
     default:
-      k_step_f32c<E2D_RIEMANN_APPROX, MINB, PFD><<<blocks, NT, sm, s>>>(kp, w_in, w_out, clk, use_clock, host_dt);
+      k_step_f32c<E2D_RIEMANN_APPROX, MINB, PFD, TMA><<<blocks, NT, sm, s>>>(kp, w_in, w_out, tm, clk, use_clock,
+                                                                        host_dt);
       break;
   }
 }
 
 cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
-                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s) {
+                             const CUtensorMap &tm_in, DevClock *clk, int use_clock, double host_dt,
+                             cudaStream_t s) {
   const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
   const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
   const int blocks = (nsx * nsy + WPB - 1) / WPB;
-  with_variant(kp.variant, [&](auto minb, auto pfd) {
-    launch_step_v<decltype(minb)::value, decltype(pfd)::value>(kp, riemann, blocks, w_in, w_out, clk, use_clock,
-                                                               host_dt, s);
+  with_variant(kp.variant, [&](auto minb, auto pfd, auto tma) {
+    launch_step_v<decltype(minb)::value, decltype(pfd)::value, decltype(tma)::value>(kp, riemann, blocks, w_in, w_out, tm_in, clk,
+                                                               use_clock, host_dt, s);
   });
   return cudaGetLastError();
+}
+
+// The TMA map of a state array: dimensions (wpitch, jsize, 8 planes), row
+// and plane strides in bytes (multiples of 16: wpitch is a multiple of 4),
+// box 64 x 1 x 8.  The encoder comes from the driver through the runtime's
+// versioned entry point (no link against the driver library).
+bool encode_f32c_map(CUtensorMap *map, const float *w, const KParams32 &kp) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if ((reinterpret_cast<uintptr_t>(w) & 15u) != 0 || (kp.wpitch & 3) != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)kp.wpitch, (cuuint64_t)kp.g.jsize, 8};
+  const cuuint64_t strides[2] = {(cuuint64_t)kp.wpitch * sizeof(float), (cuuint64_t)kp.wplane * sizeof(float)};
+  const cuuint32_t box[3] = {64, 1, 8};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(w), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 }  // namespace e2d

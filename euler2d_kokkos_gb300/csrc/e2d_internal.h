@@ -6,6 +6,7 @@
 #include <map>
 #include <string>
 
+#include <cuda.h>  // CUtensorMap (the map is encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/e2d.h"
@@ -70,6 +71,8 @@ struct KParams32 {
   long long wplane;  // wpitch * jsize
   int variant;       // step kernel register-budget variant (see launch_f32c_step)
   int strip_h;       // rows per warp strip of the step kernel
+  int wait_test;     // nonzero: strip (1, 0) never stages its first row, so its bounded
+                     // wait runs out (E2D_TEST_WAIT_TIMEOUT=1; tests the timeout path)
 };
 int default_strip_h(int nx, int ny);
 
@@ -95,6 +98,7 @@ enum : unsigned int {
   E2D_FLAG_NONFINITE = 1u,  // a state value is NaN or Inf
   E2D_FLAG_DENSITY = 2u,    // a density <= 0 was clamped to smallr
   E2D_FLAG_BAD_DT = 4u,     // the CFL wave-speed maximum is not a finite positive number
+  E2D_FLAG_TIMEOUT = 8u,    // a bounded device wait (row staging) gave up; that strip is not updated
 };
 
 // Modes of the primitives kernel.
@@ -131,21 +135,28 @@ void make_kparams32(const e2d_params &p, KParams32 *kp);
 cudaError_t configure_f32c_kernels();
 // FP32C step / batch kernel variants (register budget x row staging), see
 // with_variant in e2d_fp32c.cu.
-constexpr int kF32cVariants = 6;
+constexpr int kF32cVariants = 7;
 cudaError_t launch_f32c_from_f64(const KParams32 &kp, const double *u, float *w, cudaStream_t s);
 cudaError_t launch_f32c_to_f64(const KParams32 &kp, const float *w, double *u, cudaStream_t s);
 // CFL maximum of a state (interior) into clk->acc[slot] (slot < 0: invdt_bits).
 cudaError_t launch_f32c_dt(const KParams32 &kp, const float *w, DevClock *clk, int slot, cudaStream_t s);
 cudaError_t launch_f32c_dt_to(const KParams32 &kp, const float *w, unsigned long long *target,
                               unsigned int *status, cudaStream_t s);
+// TMA map of an FP32C state array (8 planes of wpitch x jsize floats) with a
+// box of one row: 64 columns x 1 row x 8 planes, the row ring's slot.
+// Returns false if the driver cannot encode it.
+bool encode_f32c_map(CUtensorMap *map, const float *w, const KParams32 &kp);
+// One FP32C step; tm_in: the map of w_in.
 cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in, float *w_out,
-                             DevClock *clk, int use_clock, double host_dt, cudaStream_t s);
+                             const CUtensorMap &tm_in, DevClock *clk, int use_clock, double host_dt,
+                             cudaStream_t s);
 
 // ---------------------------------------------------------------- batches
 // One instance of a batch (device table entry): its grid, its two
 // compensated states and its own time loop.  The loop state is advanced by
 // the last strip of the instance to finish each iteration.
 struct BatchInst {
+  CUtensorMap tm[2];  // TMA maps of w[0], w[1] (64-byte aligned: first member)
   KParams32 kp;
   float *w[2];
   double t, t_end, dt;          // dt: of the pending step

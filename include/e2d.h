@@ -261,7 +261,8 @@ int e2d_batch_stats(e2d_batch *b, long long *cell_updates, int *n_instances);
 int e2d_batch_stream(e2d_batch *b, void **stream);
 /* Tuning: variant of the batch kernel (0..3: at least 1, 4, 3 or 2 resident
  * blocks of 128 threads per SM with rows loaded to registers; 4, 5: 3 or 4
- * blocks with rows staged through shared memory) and rows per strip (16..512,
+ * blocks with rows staged through shared memory by cp.async; 6: 4 blocks,
+ * rows staged by TMA copies waited on with mbarriers) and rows per strip (16..512,
  * rounded up to a multiple of 16) for the size classes max(nx, ny) <= 192,
  * <= 512, > 512.  Results do not depend on them.  e2d_batch_autotune times the candidates on the live
  * batch (its iterations advance the instances) and keeps the fastest. */

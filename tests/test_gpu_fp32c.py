@@ -141,3 +141,50 @@ def test_fp32c_nonfinite_state_reports_enumeric(gpu_lib, tmp_path):
     with pytest.raises(e2d.E2DError) as ei:
         h32.step_n(10, 10.0, 0.0, 0)
     assert ei.value.status == 3  # E2D_ENUMERIC
+
+
+TMA_VARIANT = 6  # rows staged by TMA, waits on mbarriers
+
+
+def test_tma_variant_matches_default(gpu_lib, monkeypatch):
+    """The TMA-staged variant gives the same bits as the default (cp.async)
+    variant on a grid with interior, boundary and ghost-row strips."""
+    p = e2d.make_params(300, 200, problem="implode", riemann="hllc", gamma0=1.4, cfl=0.8,
+                        implode_shape=1, bc=(1, 3, 2, 1), precision=e2d.PRECISION_FP32C)
+    out = []
+    for v in ("4", str(TMA_VARIANT)):
+        monkeypatch.setenv("E2D_F32C_VARIANT", v)
+        with e2d.HydroRun(p) as h:
+            _, ns, trace = h.step_n(30, 10.0, 0.0, 0)
+            out.append((h.current(ns), trace))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_row_staging_wait_runs_out_with_etimeout(gpu_lib, monkeypatch):
+    """Failure detection without a GPU fault: with E2D_TEST_WAIT_TIMEOUT=1 the
+    TMA variant never stages the first row of strip (1, 0), so that warp's
+    bounded mbarrier wait gives up after its 1 s limit, drains its copies in
+    flight and flags the step.  step_n returns E2D_ETIMEOUT, a batch stops
+    the solve (query E2D_ETIMEOUT), and the context stays usable: the same
+    step runs normally once the switch is off."""
+    p = e2d.make_params(256, 256, problem="implode", riemann="hllc", gamma0=1.4, cfl=0.8,
+                        implode_shape=1, precision=e2d.PRECISION_FP32C)
+    monkeypatch.setenv("E2D_TEST_WAIT_TIMEOUT", "1")
+    monkeypatch.setenv("E2D_F32C_VARIANT", str(TMA_VARIANT))
+    with e2d.HydroRun(p) as h:
+        with pytest.raises(e2d.E2DError) as ei:
+            h.step_n(1, 10.0, 0.0, 0)
+        assert ei.value.status == 4  # E2D_ETIMEOUT
+    with e2d.Batch(pool_bytes=64 << 20) as b:
+        b.set_tuning(TMA_VARIANT, [64, 64, 64])
+        i = b.admit(p, 0.01)
+        b.run(1)
+        with pytest.raises(e2d.E2DError) as ei:
+            b.query(i)
+        assert ei.value.status == 4
+        _, _, active, ok = b.poll(i)
+        assert not active and not ok
+    monkeypatch.delenv("E2D_TEST_WAIT_TIMEOUT")
+    with e2d.HydroRun(p) as h:  # still the TMA variant
+        t, ns, _ = h.step_n(2, 10.0, 0.0, 0)
+        assert ns == 2 and np.isfinite(h.current(ns)).all()
