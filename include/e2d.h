@@ -220,7 +220,10 @@ int e2d_godunov_unsplit_noalloc(const e2d_params *p, double *u_in, double *u_out
  * t_end - t, runs godunov_unsplit and advances (t, nStep); steps with
  * t >= t_end do nothing.  *t and *nStep are read and updated.  dt_trace
  * (optional, n entries) receives the dt of each step taken.  Launches are
- * replayed from cached CUDA graphs.  Blocks until done. */
+ * replayed from cached CUDA graphs.  Blocks until done.  E2D_ENUMERIC: a
+ * step saw a non-finite state or dt; E2D_ETIMEOUT: a row-staging wait of the
+ * TMA variant gave up (the state of this call is incomplete; the handle stays
+ * usable). */
 int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double *dt_trace);
 
 /* ---------------------------------------------------------------------------
@@ -249,7 +252,10 @@ int e2d_batch_admit(e2d_batch *b, const e2d_params *p, double t_end, const doubl
 /* Advance every active instance by up to `iterations` steps; *n_active
  * receives the number of instances still short of their t_end. */
 int e2d_batch_run(e2d_batch *b, int iterations, int *n_active);
-/* Loop state of an instance as of the last run (t, steps, still active). */
+/* Loop state of an instance as of the last run (t, steps, still active).
+ * The outputs are filled in every case; the status is E2D_ENUMERIC or
+ * E2D_ETIMEOUT for an instance the batch stopped (a non-finite state or dt;
+ * a row-staging wait that gave up), which stays inactive. */
 int e2d_batch_query(e2d_batch *b, int id, double *t, int *nstep, int *active);
 /* Current state of an instance (hi + lo in FP64, ghosts filled), host copy. */
 int e2d_batch_get_state(e2d_batch *b, int id, double *host, int layout);
