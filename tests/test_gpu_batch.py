@@ -60,9 +60,15 @@ def test_batch_equals_single_simulation_path(gpu_lib):
 
 
 def test_batch_tuning_does_not_change_results(gpu_lib):
-    solves = small_mix(6, seed=11)
+    """Register variants, cp.async and TMA row staging (4, 6) and strip
+    heights give the same bits; the 300-wide solve has interior strips, the
+    ones TMA stages."""
+    wide = e2d.make_params(300, 96, problem="implode", riemann="hllc", gamma0=1.4, cfl=0.8,
+                           implode_shape=1, precision=e2d.PRECISION_FP32C)
+    solves = small_mix(6, seed=11) + [W.Solve("implode", wide, None, 0.02)]
     outs = []
-    for tuning in [(1, [16, 32, 64]), (0, [64, 16, 32]), (1, [8, 8, 8])]:
+    for tuning in [(1, [16, 32, 64]), (0, [64, 16, 32]), (1, [8, 8, 8]), (4, [32, 32, 32]),
+                   (6, [16, 64, 32])]:
         with e2d.Batch(pool_bytes=POOL) as b:
             b.set_tuning(*tuning)
             ids = [b.admit(s.params, s.t_end, s.u0) for s in solves]
