@@ -568,7 +568,7 @@ __device__ __forceinline__ void stage_row_tma(const KGeom &g, const CUtensorMap 
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
 template <int RS, int PFD, int TMA>
-__device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__restrict__ w_in,
+__device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
@@ -647,11 +647,13 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     return done;
   };
   // a wait that ran out: flag it, let the copies in flight land (bounded
-  // too) before the ring is reused or the block exits, leave the strip
+  // too) before the ring is reused or the block exits, leave the strip;
+  // false if a copy may still be in flight (the ring must not be reused)
   auto give_up = [&]() {
     if (lane == 0) atomicOr(status, (unsigned)E2D_FLAG_TIMEOUT);
     for (int sl = 0; sl < R; ++sl)
       if (pending & (1u << sl)) wait_slot(sl);
+    return pending == 0u;
   };
   if ((PFD > 0)) {
     // rows rb-2 .. rb+PFD-1 into slots 0 .. PFD+1 (one commit group each on
@@ -664,8 +666,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
     }
     if (bulk) {
       if (!(wait_slot(0) && wait_slot(1))) {
-        give_up();
-        return;
+        return give_up();
       }
     } else {
       cp_async_wait<(PFD > 0 ? PFD : 0)>();
@@ -695,8 +696,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       // of row m+1+PFD into that slot
       if (bulk) {
         if (!wait_slot(wrap(sm1 + 2))) {
-          give_up();
-          return;
+          return give_up();
         }
       } else {
         cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
@@ -870,6 +870,7 @@ __device__ __forceinline__ void march_strip(const KParams32 &kp, const float *__
       fold_candidate(kp, pend_term, cell, w_out, target, status);
     }
   }
+  return true;
 }
 
 extern __shared__ __align__(16) float g_ring[];
@@ -993,6 +994,7 @@ __global__ void __launch_bounds__(NT, MINB)
   __shared__ unsigned long long s_bars[TMA ? WPB * kMaxSlots : 1];  // ring slot barriers, per warp
   unsigned long long *bars = s_bars + (TMA ? (threadIdx.x >> 5) * kMaxSlots : 0);
   unsigned int phase = 0u;  // carried across the warp's strips
+  bool ring_ok = true;      // false after a TMA wait gave up with a copy maybe in flight
   if (TMA && PFD > 0) ring_bars_init(bars, PFD + 3, lane);
   for (int w = blockIdx.x * WPB + (threadIdx.x >> 5); w < total_strips; w += nwarps) {
     // instance k with strip_begin[k] <= w < strip_begin[k + 1]
@@ -1009,9 +1011,15 @@ __global__ void __launch_bounds__(NT, MINB)
     const KParams32 &kp = I.kp;
     const int par = I.par;
     const int strip = w - strip_begin[lo];
-    march_strip<RS, PFD, TMA>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
-                         strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
-                         warp_ring<PFD>(threadIdx.x >> 5), &I.tm[par], bars, phase);
+    if (ring_ok) {
+      ring_ok = march_strip<RS, PFD, TMA>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
+                                          strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
+                                          warp_ring<PFD>(threadIdx.x >> 5), &I.tm[par], bars, phase);
+    } else if (lane == 0) {
+      // a copy of an abandoned strip may still land in this warp's ring:
+      // its remaining strips are not computed, their instances stop
+      atomicOr(&I.status, (unsigned)E2D_FLAG_TIMEOUT);
+    }
     if (lane == 0) {
       __threadfence();
       const unsigned int ticket = atomicAdd(&I.done, 1u);
