@@ -2,7 +2,9 @@
 // reference's own unmodified sources against the host-only Kokkos stand-in in
 // kokkos_compat/.  Test infrastructure only: it runs the reference so that
 // the C restatement (e2d_oracle.c) and the golden fixtures can be checked
-// against it.  Built by oracle/Makefile into oracle/_ref/libe2d_ref.so.
+// against it.  Built by oracle/Makefile into oracle/_ref/libe2d_ref.so (the
+// reference's FP64 build, USE_DOUBLE) and oracle/_ref/libe2d_ref32.so (its
+// single-precision build).
 //
 // The run loop follows src/main.cpp:76-145 (compute_dt before the boundary
 // fill, the loop condition, the dt clamp at tEnd, the U/U2 ping-pong) without
@@ -44,6 +46,22 @@ store4(const HydroState & s, double * v)
 {
   for (int k = 0; k < 4; ++k)
     v[k] = s[k];
+}
+
+// The reference's real_t is double under USE_DOUBLE (libe2d_ref.so) and
+// float without it (libe2d_ref32.so); the entry points take and return FP64
+// arrays either way (a plain copy in the double build).
+void
+to_real(real_t * dst, const double * src, long n)
+{
+  for (long k = 0; k < n; ++k)
+    dst[k] = (real_t)src[k];
+}
+void
+to_double(double * dst, const real_t * src, long n)
+{
+  for (long k = 0; k < n; ++k)
+    dst[k] = (double)src[k];
 }
 
 HydroParams
@@ -123,7 +141,7 @@ extern "C"
     const long    n = (long)params.isize * params.jsize * 4;
     if (u0)
     {
-      std::memcpy(hydro.U.data(), u0, sizeof(double) * n);
+      to_real(hydro.U.data(), u0, n);
       Kokkos::deep_copy(hydro.U2, hydro.U);
     }
 
@@ -143,9 +161,9 @@ extern "C"
       ns++;
       t += dt;
     }
-    const double * cur = (ns % 2 == 0) ? hydro.U.data() : hydro.U2.data();
+    const real_t * cur = (ns % 2 == 0) ? hydro.U.data() : hydro.U2.data();
     if (u_out)
-      std::memcpy(u_out, cur, sizeof(double) * n);
+      to_double(u_out, cur, n);
     *nstep = ns;
     *t_out = t;
     return 0;
@@ -160,7 +178,7 @@ extern "C"
     HydroParams params;
     params.setup(cm);
     HydroRun<Dev> hydro(params, cm);
-    std::memcpy(u_out, hydro.U.data(), sizeof(double) * (long)params.isize * params.jsize * 4);
+    to_double(u_out, hydro.U.data(), (long)params.isize * params.jsize * 4);
     return 0;
   }
 
@@ -173,9 +191,9 @@ extern "C"
     params.setup(cm);
     HydroRun<Dev> hydro(params, cm);
     const long    n = (long)params.isize * params.jsize * 4;
-    std::memcpy(hydro.U.data(), u, sizeof(double) * n);
+    to_real(hydro.U.data(), u, n);
     hydro.make_boundaries(hydro.U);
-    std::memcpy(u, hydro.U.data(), sizeof(double) * n);
+    to_double(u, hydro.U.data(), n);
     return 0;
   }
 
@@ -192,7 +210,7 @@ extern "C"
     HydroParams params;
     params.setup(cm);
     DataArray<Dev> U("U", params.isize, params.jsize);
-    std::memcpy(U.data(), u, sizeof(double) * (long)params.isize * params.jsize * 4);
+    to_real(U.data(), u, (long)params.isize * params.jsize * 4);
     char cwd[4096];
     if (!getcwd(cwd, sizeof cwd) || chdir(outdir) != 0)
       return 1;
@@ -211,7 +229,7 @@ extern "C"
     HydroParams params;
     params.setup(cm);
     HydroRun<Dev> hydro(params, cm);
-    std::memcpy(hydro.U.data(), u, sizeof(double) * (long)params.isize * params.jsize * 4);
+    to_real(hydro.U.data(), u, (long)params.isize * params.jsize * 4);
     return hydro.compute_dt(0);
   }
 
@@ -223,7 +241,9 @@ extern "C"
     for (int k = 0; k < n; ++k)
     {
       HydroState qs;
-      f.computePrimitives(load4(u + 4 * k), c + k, qs);
+      real_t     ck;
+      f.computePrimitives(load4(u + 4 * k), &ck, qs);
+      c[k] = ck;
       store4(qs, q + 4 * k);
     }
   }

@@ -197,3 +197,18 @@ def oracle_kwargs(text: str) -> dict:
 def run_limits(text: str):
     m = parse_ini(text)
     return int(m.get("run.nstepmax", 1000)), f32(float(m.get("run.tend", 0.0)))
+
+
+# A four-quadrant flow with drawn states (416 x 1824 cells, absorbing walls,
+# split at 0.5, gamma 1.4, HLLC, CFL 0.8) on which FP32 arithmetic breaks
+# down: the FP32C state turns non-finite near t = 0.048 on the column of the
+# vertical split, and so does the reference's own single-precision build,
+# near t = 0.05; FP64 runs it to the end (667 steps).
+BREAKDOWN_NX, BREAKDOWN_NY = 416, 1824
+BREAKDOWN_T_END = 0.07696256392150672
+BREAKDOWN_STATES = [
+    [1.4045364949998327, 1.2478185891339812, 1.0125626194788715, 1.4112208957238694],
+    [0.5510051598548608, 1.3033349919491264, 1.4899767690701817, 0.8116696708168066],
+    [1.9604589210178323, 0.12702456455098715, -1.1540322213586327, -0.050099086017271144],
+    [1.3025418760856602, 1.7962252840716093, 0.2289799732296557, -1.1532139468078726],
+]

@@ -4,6 +4,8 @@ admission follows the pool's free bytes."""
 import numpy as np
 import pytest
 
+import _cases as C
+
 import euler2d_kokkos_gb300 as e2d
 from euler2d_kokkos_gb300 import workloads as W
 
@@ -276,18 +278,7 @@ def test_serving_nonfinite_policies(gpu_lib):
         assert st.wasted_cell_updates > 0 and st.cell_updates == good_updates, policy
 
 
-# A four-quadrant flow with drawn states (416 x 1824 cells, reflecting walls,
-# split at 0.5) on which FP32 arithmetic breaks down: the FP32C state turns
-# non-finite near t = 0.048 on the column of the vertical split, where the
-# reference's own single-precision build (USE_DOUBLE off) also turns
-# non-finite, near t = 0.05; FP64 runs it to the end.
-BREAKDOWN_T_END = 0.07696256392150672
-BREAKDOWN_STATES = [
-    [1.4045364949998327, 1.2478185891339812, 1.0125626194788715, 1.4112208957238694],
-    [0.5510051598548608, 1.3033349919491264, 1.4899767690701817, 0.8116696708168066],
-    [1.9604589210178323, 0.12702456455098715, -1.1540322213586327, -0.050099086017271144],
-    [1.3025418760856602, 1.7962252840716093, 0.2289799732296557, -1.1532139468078726],
-]
+BREAKDOWN_T_END, BREAKDOWN_STATES = C.BREAKDOWN_T_END, C.BREAKDOWN_STATES
 
 
 def test_fp32_breakdown_is_rerun_in_fp64(gpu_lib):
