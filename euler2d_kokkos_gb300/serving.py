@@ -13,7 +13,8 @@ serve            -- continuous batching under open-loop Poisson arrivals:
                     request's latency (arrival to completion) is recorded.
 
 A FP32C solve whose state turns non-finite is stopped by the batch
-(E2D_ENUMERIC) without affecting the others.  With on_nonfinite="fp64" (the
+(E2D_ENUMERIC; E2D_ETIMEOUT for a row-staging wait of the TMA variant that
+gave up) without affecting the others.  With on_nonfinite="fp64" (the
 default) it is admitted again from its initial state as an FP64 instance --
 the bit-exact FP64 kernels, in the same batch -- and its latency runs from the
 original arrival; "drop" records it in RunStats.failed instead.  FP32 arithmetic
@@ -38,7 +39,7 @@ class RunStats:
     iterations: int = 0
     latencies: list = field(default_factory=list)
     tuning: tuple = ()
-    failed: list = field(default_factory=list)     # indices of solves stopped by a non-finite state
+    failed: list = field(default_factory=list)     # indices of solves stopped for good
     escalated: list = field(default_factory=list)  # indices of FP32C solves re-run in FP64
     wasted_cell_updates: int = 0                   # updates of stopped solves (not in cell_updates)
 
