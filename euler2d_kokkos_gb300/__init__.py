@@ -326,13 +326,19 @@ class HydroRun:
     # -- the device-resident time loop
     def step_n(self, n: int, t_end: float, t: float, nstep: int, want_trace: bool = True):
         """Up to n steps of the src/main.cpp loop on the device.
-        Returns (t, nstep, dt_trace)."""
+        Returns (t, nstep, dt_trace).  An E2DError raised for a stopped run
+        (E2D_ENUMERIC, E2D_ETIMEOUT) carries .t and .nstep: where the loop
+        state stands."""
         tt = ctypes.c_double(t)
         ns = ctypes.c_int(nstep)
         trace = np.zeros(max(int(n), 1)) if want_trace else None
-        _check(self._lib.e2d_step_n(self._h, int(n), float(t_end), ctypes.byref(tt), ctypes.byref(ns),
-                                    trace.ctypes.data if trace is not None else None),
-               "step_n", self._h)
+        try:
+            _check(self._lib.e2d_step_n(self._h, int(n), float(t_end), ctypes.byref(tt), ctypes.byref(ns),
+                                        trace.ctypes.data if trace is not None else None),
+                   "step_n", self._h)
+        except E2DError as e:
+            e.t, e.nstep = tt.value, ns.value
+            raise
         taken = ns.value - nstep
         return tt.value, ns.value, (trace[:taken] if trace is not None else None)
 

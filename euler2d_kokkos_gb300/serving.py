@@ -153,25 +153,49 @@ def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, k
     return stats, states
 
 
-def run_one_at_a_time(solves, chunk=256):
+def _solve_alone(params, s, chunk):
+    """One solve on its own handle to its t_end; returns the steps taken.
+    A stopped run raises step_n's E2DError (its .nstep: the steps taken)."""
+    with HydroRun(params, init_problem=s.u0 is None) as h:
+        if s.u0 is not None:
+            h.set_state(0, s.u0)
+        t, ns = 0.0, 0
+        while t < s.t_end:
+            prev = ns
+            t, ns, _ = h.step_n(chunk, s.t_end, t, ns, want_trace=False)
+            if ns == prev:
+                break
+        h.current(ns)
+        return ns
+
+
+def run_one_at_a_time(solves, chunk=256, on_nonfinite="fp64"):
     """Each solve alone: its own simulation handle, the device time loop in
-    graph-replayed chunks until t_end, its result read back."""
+    graph-replayed chunks until t_end, its result read back.  A FP32C solve
+    that stops (E2D_ENUMERIC / E2D_ETIMEOUT) is handled as run_batched
+    handles it: re-run in FP64 ("fp64") or recorded as failed ("drop")."""
     stats = RunStats()
+    reaper = _Reaper(solves, stats, on_nonfinite)
     _sync_device()
     t0 = time.perf_counter()
-    for s in solves:
-        with HydroRun(s.params, init_problem=s.u0 is None) as h:
-            if s.u0 is not None:
-                h.set_state(0, s.u0)
-            t, ns = 0.0, 0
-            while t < s.t_end:
-                prev = ns
-                t, ns, _ = h.step_n(chunk, s.t_end, t, ns, want_trace=False)
-                if ns == prev:
-                    break
-            h.current(ns)
-            stats.cell_updates += ns * s.params.nx * s.params.ny
+    for k, s in enumerate(solves):
+        p = s.params
+        while True:
+            try:
+                ns = _solve_alone(reaper.params(k), s, chunk)
+            except E2DError as e:
+                if e.status not in (3, 4):  # E2D_ENUMERIC, E2D_ETIMEOUT
+                    raise
+                stats.wasted_cell_updates += e.nstep * p.nx * p.ny
+                if reaper.policy == "fp64" and p.precision == PRECISION_FP32C and k not in reaper.fp64:
+                    reaper.fp64.add(k)
+                    stats.escalated.append(k)
+                    continue
+                stats.failed.append(k)
+                break
+            stats.cell_updates += ns * p.nx * p.ny
             stats.solves += 1
+            break
     stats.seconds = time.perf_counter() - t0
     return stats
 

@@ -70,3 +70,43 @@ def test_fp64_failure_and_drop_policy_are_not_rerun():
 def test_unknown_policy_is_refused():
     with pytest.raises(ValueError):
         serving._Reaper([], serving.RunStats(), "retry")
+
+
+class FakeRun:
+    """HydroRun stand-in: FP32C runs stop with E2D_ENUMERIC after 5 steps,
+    FP64 runs reach t_end in 7."""
+
+    def __init__(self, params, init_problem=True):
+        self.p = params
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+    def set_state(self, which, u):
+        pass
+
+    def step_n(self, n, t_end, t, nstep, want_trace=True):
+        if self.p.precision == e2d.PRECISION_FP32C:
+            err = e2d.E2DError(3, "step_n")
+            err.t, err.nstep = 0.01, nstep + 5
+            raise err
+        return t_end, nstep + 7, None
+
+    def current(self, nstep):
+        return None
+
+
+def test_one_at_a_time_applies_the_same_policy(monkeypatch):
+    monkeypatch.setattr(serving, "HydroRun", FakeRun)
+    sv = solves(e2d.PRECISION_FP32C)
+    cells = [s.params.nx * s.params.ny for s in sv]
+    st = serving.run_one_at_a_time(sv)
+    assert st.solves == 2 and st.escalated == [0, 1] and st.failed == []
+    assert st.cell_updates == 7 * sum(cells) and st.wasted_cell_updates == 5 * sum(cells)
+    st = serving.run_one_at_a_time(sv, on_nonfinite="drop")
+    assert st.solves == 0 and st.failed == [0, 1] and st.escalated == []
+    st = serving.run_one_at_a_time(solves(e2d.PRECISION_FP64))
+    assert st.solves == 2 and st.escalated == [] and st.wasted_cell_updates == 0
