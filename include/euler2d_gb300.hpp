@@ -203,6 +203,16 @@ class Batch {
     ck(e2d_batch_query(b_, id, t, nstep, &a), "Batch::query");
     return a != 0;
   }
+  // like active() without throwing for a solve the batch stopped: returns
+  // E2D_OK, E2D_ENUMERIC (non-finite state or dt) or E2D_ETIMEOUT (a
+  // row-staging wait gave up); *active, *t, *nstep are filled in every case
+  int poll(int id, bool *active, double *t = nullptr, int *nstep = nullptr) {
+    int a = 0;
+    const int rc = e2d_batch_query(b_, id, t, nstep, &a);
+    if (rc != E2D_OK && rc != E2D_ENUMERIC && rc != E2D_ETIMEOUT) ck(rc, "Batch::poll");
+    if (active) *active = a != 0;
+    return rc;
+  }
   std::vector<double> state(int id, const HydroParams &p) {
     std::vector<double> u((size_t)4 * p.isize * p.jsize);
     ck(e2d_batch_get_state(b_, id, u.data(), E2D_LAYOUT_LEFT), "Batch::get_state");

@@ -183,6 +183,8 @@ int main(int argc, char **argv) {
   const int id = batch.admit(params, 0.1);
   while (batch.run(16) > 0) {
   }
+  bool active = true;
+  if (batch.poll(id, &active) != E2D_OK) return 2;
   std::vector<double> u = batch.state(id, params);
   batch.release(id);
   return argc + (int)u.size() > 0 ? 0 : 1;
