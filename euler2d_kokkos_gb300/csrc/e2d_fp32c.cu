@@ -1240,15 +1240,16 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
 // box 64 x 1 x 8.  The encoder comes from the driver through the runtime's
 // versioned entry point (no link against the driver library).
 bool encode_f32c_map(CUtensorMap *map, const float *w, const KParams32 &kp) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
+  // looked up once (thread-safe static initialisation); null if unavailable
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess || !fn)
-      return false;
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+        q != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
   if ((reinterpret_cast<uintptr_t>(w) & 15u) != 0 || (kp.wpitch & 3) != 0) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)kp.wpitch, (cuuint64_t)kp.g.jsize, 8};
   const cuuint64_t strides[2] = {(cuuint64_t)kp.wpitch * sizeof(float), (cuuint64_t)kp.wplane * sizeof(float)};
