@@ -428,9 +428,12 @@ def batch_summary(instances, sample, fp64=False):
             "tuning": {"variant": bstats.tuning[0], "strip_h_per_class": bstats.tuning[1]},
             "value": bstats.gcell_per_s, "unit": METRIC,
             "batched": {"value": bstats.gcell_per_s, "seconds": bstats.seconds,
-                        "cell_updates": bstats.cell_updates, "launch_iterations": bstats.iterations},
+                        "cell_updates": bstats.cell_updates, "launch_iterations": bstats.iterations,
+                        "rerun_fp64_after_nonfinite": list(bstats.escalated), "failed": list(bstats.failed)},
             "one_at_a_time": {"value": seq.gcell_per_s, "seconds": seq.seconds, "solves": seq.solves,
                               "cell_updates": seq.cell_updates,
+                              "rerun_fp64_after_nonfinite": [sample_idx[k] for k in seq.escalated],
+                              "failed": [sample_idx[k] for k in seq.failed],
                               "sample": f"{len(sample_idx)} of the {len(solves)} solves, every {stride}th"},
             "batched_over_one_at_a_time": bstats.gcell_per_s / seq.gcell_per_s if seq.gcell_per_s else None,
             **out_l1}
