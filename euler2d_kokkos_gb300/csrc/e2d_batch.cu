@@ -357,7 +357,9 @@ int e2d_batch_create(int riemann, size_t pool_bytes, int max_instances, e2d_batc
   if (cudaMemsetAsync(b->d_insts, 0, sizeof(BatchInst) * (size_t)max_instances, b->stream) != cudaSuccess ||
       cudaMemsetAsync(b->d_insts64, 0, sizeof(BatchInst64) * (size_t)max_instances, b->stream) != cudaSuccess)
     return fail(E2D_ECUDA);
-  if (configure_f64_kernels() != cudaSuccess) return fail(E2D_ECUDA);
+  // shared-memory limits of the kernels (idempotent; a batch may be the
+  // process's first handle)
+  if (configure_f64_kernels() != cudaSuccess || configure_f32c_kernels() != cudaSuccess) return fail(E2D_ECUDA);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return fail(E2D_ECUDA);
   *out = b;
   return E2D_OK;
