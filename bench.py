@@ -11,7 +11,9 @@ from HBM.
 Secondary (in the same JSON line, key "fp32c"): the 8192x8192 four-quadrant
 Riemann problem (Lax-Liu 3 split at 0.5, absorbing walls, HLLC, CFL 0.8) in
 the FP32 compensated mode, with its relative L1 density error against the
-FP64 path (which is bit-identical to the reference) at 1024x1024, t = 0.3.
+FP64 path (which is bit-identical to the reference) on the same 8192x8192
+grid after the same number of steps as the timed run, and at 1024x1024 to
+t = 0.3.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--precision fp64|fp32c] [--problem blast|four_quadrant] [--nx N]
@@ -56,11 +58,13 @@ def parse():
                     help="steps of the CPU baseline sample (0: sized to ~15 s)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "c3"],
+    ap.add_argument("--mode", default="step", choices=["step", "batch", "serve", "c3", "f64tiles", "fp64peak"],
                     help="step: one grid (default); batch: 512 mixed solves batched vs one at a "
                          "time; serve: Poisson arrivals into the batched loop; c3: the 8192^2 "
                          "four-quadrant problem to t = 0.3 in FP32C, in FP64 and in FP64 from a perturbed "
-                         "initial state (about 40 min at 8192^2, 5 min at 4096^2)")
+                         "initial state (about 40 min at 8192^2, 5 min at 4096^2); f64tiles: the FP64 "
+                         "step at every tile shape, fused and as two launches; fp64peak: the FP64 "
+                         "operation rates of this GPU")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--sample", type=int, default=24, help="solves timed one at a time (batch mode)")
     ap.add_argument("--rates", default="", help="arrival rates (solves/s) for serve mode, comma-separated")
@@ -261,7 +265,22 @@ def max_over_ranks(dist, x: float) -> float:
 
 
 def measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
-            with_e2e=True, with_clocks=True, riemann=None):
+            with_e2e=True, with_clocks=True, riemann=None, env=None):
+    saved = {k: os.environ.get(k) for k in (env or {})}
+    os.environ.update(env or {})  # read by the library when a handle is created
+    try:
+        return _measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
+                        with_e2e, with_clocks, riemann)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def _measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, barrier, dist,
+             with_e2e, with_clocks, riemann):
     p = workload_params(e2d, problem, nx, riemann or args.riemann, precision)
     h = e2d.HydroRun(p)
     stream = torch.cuda.ExternalStream(h.stream())
@@ -343,15 +362,74 @@ def roofline(kt, precision, cells, prefix):
     return r
 
 
-def fp64_pipe_info(kt, cells):
-    path = os.path.join(ROOT, "profiles", "fp64_peak.json")
-    if not os.path.exists(path):
+# FP64 operations of the fused FP64 step (k_step_f64 in
+# euler2d_kokkos_gb300/csrc/e2d_fp64.cu), counted from its source.  Adds,
+# subtracts and multiplies count 1 each (the FP64 pipe runs them at its FMA
+# rate); divisions and square roots are counted apart and weighted by their
+# measured cost (FMA rate / their rate); fmax and comparisons by theirs.
+# Limiter min/max, sign tests, cut-offs against positive constants and the
+# exact scalings by 0.5 and 2 run on the integer pipe and are not counted.
+F64_OPS = {
+    # stage 2, per cell of the tile and of its 1-cell ring: 8 limited slopes
+    # (3 subtractions each, f64x::slope_limited) and the trace sources
+    # (trace_sources: 3 + 3 + 2 + 2 products, 3 + 3 + 2 + 2 sums less one
+    # shared dux + dvy; dpx / r and dpy / r)
+    "slopes_trace": {"simple": 24 + 20, "div": 2},
+    # face_pair for the 4 variables of one direction: s0 * dtd, then
+    # q - h + sx and q + h + sx
+    "faces_dir": {"simple": 4 * 5},
+    # stage 3, one solve plus the 4 products by dt/dx
+    "hllc": {"simple": 51 + 4, "div": 6, "sqrt": 2},
+    "hll": {"simple": 64 + 4, "div": 3, "sqrt": 2},
+    # epilogue per cell: the update (4 x 4 sums), primitives (7 + 3
+    # divisions), the CFL term (6 + a division and a square root), and
+    # fmax / comparisons (the running maximum, the dx / dy power-of-two
+    # tests, the density test, the block fold's shuffles, ~6)
+    "epilogue": {"simple": 16 + 7 + 6, "div": 3 + 1, "sqrt": 1, "max": 6},
+}
+F64_TILES = {0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}
+
+
+def fp64_ops_per_cell(riemann, tile=0):
+    """FP64 operations per cell-update of the fused step by kind, for a tile
+    shape: per tile, (TX+2)(TY+2)-4 slope/trace evaluations, 2 TX TY + 2 TX
+    + 2 TY face-pair directions, (TX+1) TY + TX (TY+1) solves and TX TY
+    epilogues.  None for the iterative approx solver."""
+    if riemann not in F64_OPS:
         return None
-    d = json.load(open(path))
-    out = {"dfma_peak_gops": d.get("dfma_gops")}
-    busy = d.get("fp64_pipe_busy_pct")
-    if busy:
-        out["fp64_pipe_busy_pct_ncu"] = busy
+    tx, ty = F64_TILES.get(tile, (32, 32))
+    n = {"slopes_trace": (tx + 2) * (ty + 2) - 4, "faces_dir": 2 * tx * ty + 2 * tx + 2 * ty,
+         riemann: (tx + 1) * ty + tx * (ty + 1), "epilogue": tx * ty}
+    tot = {"simple": 0.0, "div": 0.0, "sqrt": 0.0, "max": 0.0}
+    for part, cnt in n.items():
+        for kind, v in F64_OPS[part].items():
+            tot[kind] += cnt * v / (tx * ty)
+    return tot
+
+
+_FP64_RATES = None
+
+
+def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0):
+    """FP64-pipe roofline of the fused step, live: the probe's measured rates
+    (e2d_fp64_rates, this run), the source-counted operations per cell in FMA
+    equivalents, and the fraction of the FMA peak the kernel sustained."""
+    global _FP64_RATES
+    if _FP64_RATES is None:
+        _FP64_RATES = e2d.fp64_rates()
+    r = _FP64_RATES
+    ops = fp64_ops_per_cell(riemann, tile)
+    out = {"rates_gops": r, "peak_gops": r["fma"], "unit": "G FP64 FMA-equivalent ops/s",
+           "peak_source": "e2d_fp64_rates probe in this run (8 chains/thread, 8x256 threads/SM, CUDA events)"}
+    if not ops:
+        return out
+    cost = {"simple": 1.0, "div": r["fma"] / r["div"], "sqrt": r["fma"] / r["sqrt"], "max": r["fma"] / r["max"]}
+    per_cell = sum(ops[k] * cost[k] for k in ops)
+    achieved = per_cell * cells / (kernel_ms * 1e-3) / 1e9
+    out.update({"ops_per_cell": ops, "fma_equivalent_per_cell": per_cell,
+                "cost_in_fma": {"div": cost["div"], "sqrt": cost["sqrt"], "max": cost["max"]},
+                "achieved_gops": achieved, "frac": achieved / r["fma"],
+                "ops_source": "counted from k_step_f64's source (bench.py F64_OPS)"})
     return out
 
 
@@ -375,6 +453,27 @@ def l1_check(e2d, nx, t_end, problem="four_quadrant"):
     for h, _, _ in hs.values():
         h.close()
     return res
+
+
+def l1_steps(e2d, problem, nx, steps):
+    """FP32C vs FP64 (bit-identical to the reference) on the bench's own
+    workload: the same initial state advanced `steps` steps of the device time
+    loop at nx^2; relative L1 of density (FP64 accumulation) and the largest
+    relative difference of the dt sequences."""
+    out = {}
+    for prec in ("fp64", "fp32c"):
+        h = e2d.HydroRun(workload_params(e2d, problem, nx, "hllc", prec))
+        t, ns, tr = h.step_n(steps, 10.0, 0.0, 0)
+        out[prec] = (h, t, ns, np.asarray(tr))
+    (h64, t64, n64, tr64), (h32, t32, n32, tr32) = out["fp64"], out["fp32c"]
+    d, r = h32.l1_diff(n32 % 2, h64, n64 % 2, e2d.ID)  # on the device, FP64 sums
+    h32.close()
+    h64.close()
+    n = min(len(tr64), len(tr32))
+    return {"grid": f"{nx}x{nx}", "steps": n32, "steps_fp64": n64, "t_fp32c": t32, "t_fp64": t64,
+            "rel_l1_density_vs_fp64": d / r,
+            "dt_max_rel_diff": float(np.max(np.abs(tr32[:n] - tr64[:n]) / tr64[:n])) if n else None,
+            "oracle": "FP64 GPU path (bit-identical to the reference), same initial state and step count"}
 
 
 def fp64_l1_of(e2d, solve, got):
@@ -540,6 +639,46 @@ def c3_mode(args):
     print(json.dumps(line), flush=True)
 
 
+def f64tiles_mode(args):
+    """The FP64 blast (--nx, HLLC and HLL) at every fused-step tile shape and
+    as two launches per step, CUDA events on the library's stream."""
+    import torch
+
+    import euler2d_kokkos_gb300 as e2d
+
+    nx = args.nx
+    cells = nx * nx
+    bar = torch.cuda.synchronize
+    rows = []
+    with ClockSampler(0) as clocks:
+        for rs in ("hllc", "hll"):
+            for label, env in [("fused 32x32", {"E2D_F64_TILE": "0"}), ("fused 32x16", {"E2D_F64_TILE": "1"}),
+                               ("fused 32x31", {"E2D_F64_TILE": "2"}), ("fused 32x15", {"E2D_F64_TILE": "3"}),
+                               ("two launches 32x32", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"})]:
+                m = measure(e2d, torch, args, "fp64", "blast", nx, args.steps, args.warmup, 0, bar, None,
+                            with_e2e=False, with_clocks=False, riemann=rs, env=env)
+                kt = {k: round(v[0] / v[1], 4) for k, v in m["kernels"].items()}
+                row = {"riemann": rs, "form": label, "ms_per_step": m["ms"] / args.steps,
+                       "gcell_per_s": cells * args.steps / (m["ms"] / 1e3) / 1e9, "kernel_ms_avg": kt}
+                if label.startswith("fused"):
+                    k = next(k for k in kt if k.startswith("k_step_f64"))
+                    row["fp64_pipe"] = fp64_pipe_info(e2d, rs, kt[k], cells, int(env["E2D_F64_TILE"]))
+                rows.append(row)
+    line = {"metric": METRIC, "mode": "f64tiles", "config": config("blast", nx, "hllc/hll", "fp64"),
+            "steps": args.steps, "rows": rows, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def fp64peak_mode(args):
+    import euler2d_kokkos_gb300 as e2d
+
+    with ClockSampler(0) as clocks:
+        rates = [e2d.fp64_rates() for _ in range(3)]
+    best = {k: max(r[k] for r in rates) for k in rates[0]}
+    print(json.dumps({"mode": "fp64peak", "unit": "G FP64 operations/s", "rates": best, "runs": rates,
+                      "clocks": clocks.summary()}), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -557,6 +696,10 @@ def main():
     if args.mode == "c3":
         if rank == 0:
             c3_mode(args)
+        return
+    if args.mode in ("f64tiles", "fp64peak"):
+        if rank == 0:
+            (f64tiles_mode if args.mode == "f64tiles" else fp64peak_mode)(args)
         return
 
     import torch
@@ -582,11 +725,12 @@ def main():
                 barrier, dist)
     value = cells * args.steps * world / (m["ms"] / 1e3) / 1e9
     kt = m["kernels"]
-    prefix = "k_flux_update" if args.precision == "fp64" else "k_step_f32c"
+    prefix = "k_step_f64" if args.precision == "fp64" else "k_step_f32c"
     roof = roofline(kt, args.precision, cells, prefix)
     if roof and args.precision == "fp64":
         roof["note"] = "the FP64 step is bound by GB300's FP64 pipe, not HBM: see fp64_pipe"
-        roof["fp64_pipe"] = fp64_pipe_info(kt, cells)
+        roof["fp64_pipe"] = fp64_pipe_info(e2d, args.riemann, roof["kernel_ms_avg"], cells,
+                                           int(os.environ.get("E2D_F64_TILE", "0")))
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -609,7 +753,8 @@ def main():
             "value": sc * args.steps / (s["ms"] / 1e3) / 1e9, "unit": METRIC,
             "ms_per_step": s["ms"] / args.steps,
             "roofline": roofline(s["kernels"], "fp32c", sc, "k_step_f32c"),
-            "accuracy": l1_check(e2d, 1024, 0.3)}
+            "accuracy": {**l1_steps(e2d, "four_quadrant", 8192, args.steps),
+                         "to_t_0.3_at_1024": l1_check(e2d, 1024, 0.3)}}
         # the C2 blast in the FP32 compensated mode, with its error against FP64
         sb = measure(e2d, torch, args, "fp32c", args.problem, nx, args.steps, args.warmup, local,
                      barrier, None, with_e2e=False, with_clocks=False)
@@ -618,14 +763,27 @@ def main():
             "value": cells * args.steps / (sb["ms"] / 1e3) / 1e9, "unit": METRIC,
             "ms_per_step": sb["ms"] / args.steps,
             "roofline": roofline(sb["kernels"], "fp32c", cells, "k_step_f32c"),
-            "accuracy": l1_check(e2d, 1024, 0.05, args.problem)}
+            "accuracy": {**l1_steps(e2d, args.problem, nx, args.steps),
+                         "to_t_0.05_at_1024": l1_check(e2d, 1024, 0.05, args.problem)}}
         # C2 also names the HLL solver: the same FP64 blast with it
         hl = measure(e2d, torch, args, "fp64", args.problem, nx, args.steps, args.warmup, local,
                      barrier, None, with_e2e=False, with_clocks=False, riemann="hll")
+        rh = roofline(hl["kernels"], "fp64", cells, "k_step_f64")
+        if rh:
+            rh["fp64_pipe"] = fp64_pipe_info(e2d, "hll", rh["kernel_ms_avg"], cells)
         line["hll"] = {"config": config(args.problem, nx, "hll", "fp64"),
                        "value": cells * args.steps / (hl["ms"] / 1e3) / 1e9, "unit": METRIC,
-                       "ms_per_step": hl["ms"] / args.steps,
-                       "roofline": roofline(hl["kernels"], "fp64", cells, "k_flux_update")}
+                       "ms_per_step": hl["ms"] / args.steps, "roofline": rh}
+        # the same FP64 step as two launches (fill + flux/update; the
+        # primitives array round-trips through HBM), against the fused step
+        tl = measure(e2d, torch, args, "fp64", args.problem, nx, args.steps, args.warmup, local,
+                     barrier, None, with_e2e=False, with_clocks=False, env={"E2D_F64_SPLIT": "1"})
+        line["fp64_two_launch"] = {
+            "config": config(args.problem, nx, args.riemann, "fp64"),
+            "value": cells * args.steps / (tl["ms"] / 1e3) / 1e9, "unit": METRIC,
+            "ms_per_step": tl["ms"] / args.steps,
+            "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in tl["kernels"].items()},
+            "fused_over_two_launch": (tl["ms"] / m["ms"])}
         # batched mixed solves against one at a time, and one loaded serving point
         line["batch"] = batch_summary(512, 24)
         line["batch_fp64"] = batch_summary(64, 8, fp64=True)

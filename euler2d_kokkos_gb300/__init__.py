@@ -99,6 +99,8 @@ SIGNATURES = {
     "e2d_ini_get_string": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
                             ctypes.c_char_p, ctypes.c_size_t], _I),
     "e2d_save_vtk": ([_V, _I, ctypes.c_char_p], _I),
+    "e2d_write_vtk": ([_P, _V, _I, ctypes.c_char_p], _I),
+    "e2d_fp64_rates": ([_V], _I),
     "e2d_create": ([_P, ctypes.POINTER(_V)], _I),
     "e2d_destroy": ([_V], _I),
     "e2d_last_error": ([_V], ctypes.c_char_p),
@@ -292,6 +294,11 @@ class HydroRun:
                            else (self.params.isize, self.params.jsize, 4), dtype=np.float64)
         _check(self._lib.e2d_get_state(self._h, int(which), out.ctypes.data, layout), "e2d_get_state", self._h)
         return out
+
+    def save_vtk(self, which: int, filename: str) -> None:
+        """HydroRun::saveVTK (src/HydroRun.h:506-609): state `which` as an
+        ASCII .vti file of the interior cells, the reference's text format."""
+        _check(self._lib.e2d_save_vtk(self._h, int(which), os.fsencode(filename)), "e2d_save_vtk", self._h)
 
     @property
     def U(self) -> np.ndarray:
@@ -504,6 +511,26 @@ class Batch:
 EVAL = {"primitives": (0, 4, 5), "slopes": (1, 20, 8), "trace_xmin": (2, 12, 4), "trace_xmax": (3, 12, 4),
         "trace_ymin": (4, 12, 4), "trace_ymax": (5, 12, 4), "riemann_approx": (6, 8, 4),
         "riemann_hll": (7, 8, 4), "riemann_hllc": (8, 8, 4)}
+
+
+def write_vtk(params: HydroParams, u: np.ndarray, filename: str, layout: int = LAYOUT_LEFT) -> None:
+    """The .vti text writer of HydroRun::saveVTK (src/HydroRun.h:546-607)
+    for a host state (ghosts included); no device work."""
+    a = np.ascontiguousarray(u, dtype=np.float64)
+    if a.size != 4 * params.isize * params.jsize:
+        raise ValueError(f"state has {a.size} values, expected {4 * params.isize * params.jsize}")
+    _check(load_library().e2d_write_vtk(ctypes.byref(params._raw), a.ctypes.data, int(layout),
+                                        os.fsencode(filename)), "write_vtk")
+
+
+FP64_RATE_NAMES = ("fma", "add", "mul", "div", "sqrt", "max")
+
+
+def fp64_rates() -> dict:
+    """Measured G operations/s of this GPU's FP64 operations (e2d_fp64_rates)."""
+    out = np.zeros(6)
+    _check(load_library().e2d_fp64_rates(out.ctypes.data), "fp64_rates")
+    return dict(zip(FP64_RATE_NAMES, out.tolist()))
 
 
 def save_npy(path: str, data) -> None:

@@ -22,7 +22,11 @@ struct e2d_sim {
   int device = 0;
   cudaStream_t stream = nullptr;
   double *U[2] = {nullptr, nullptr};  // FP64: U and U2 of the reference
-  double *Q = nullptr;                // FP64: primitives scratch (one full array)
+  double *Q[2] = {nullptr, nullptr};  // FP64: primitives of U and of U2 (the fused step's ping-pong;
+                                      // Q[0] is the two-launch step's scratch)
+  CUtensorMap QTM[2];                 // FP64: TMA maps of Q[0], Q[1] (fused step's tile staging)
+  int q_tma = 0;                      // FP64: both maps encoded (isize even)
+  int f64_split = 0;                  // FP64 device loop as two launches per step (E2D_F64_SPLIT=1)
   float *W[2] = {nullptr, nullptr};   // FP32C: compensated U and U2 (8 float planes)
   CUtensorMap TM[2];                  // FP32C: TMA maps of W[0], W[1] (row staging)
   double *stage = nullptr;            // FP32C: FP64 staging array (set/get/init)
@@ -98,6 +102,8 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->ph.inv_dy_pow2 = inv_pow2(p.dy);
   kp->tile = 0;
   if (const char *v = std::getenv("E2D_F64_TILE")) kp->tile = std::atoi(v);
+  const char *wt = std::getenv("E2D_TEST_WAIT_TIMEOUT");
+  kp->wait_test = (wt && std::atoi(wt) != 0) ? 1 : 0;
 }
 
 namespace {
@@ -128,11 +134,21 @@ cudaError_t enqueue_step(e2d_sim *s, int par) {
     return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 1,
                             0.0, s->stream);
   double *in = s->U[par], *out = s->U[par ^ 1];
+  if (!s->f64_split)
+    return launch_step_f64(s->kp, s->p.riemannSolverType, s->QTM[par], s->q_tma, s->Q[par], s->Q[par ^ 1], in,
+                           out, s->clk, s->dt_trace, s->stream);
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK;
-  cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream);
+  cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q[0], s->clk, mode, s->stream);
   if (e != cudaSuccess) return e;
-  return launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 1, 0.0,
+  return launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q[0], in, out, s->clk, 1, 0.0,
                                 s->dt_trace, s->stream);
+}
+
+// Before the fused FP64 steps of a device-loop call: the primitives of the
+// input state and its CFL maximum, which the first step reads.
+cudaError_t enqueue_prologue(e2d_sim *s, int par, int nstep) {
+  if (s->fp32 || s->f64_split) return cudaSuccess;
+  return launch_fill_f64(s->kp, s->U[par], nullptr, s->Q[par], s->clk, FILL_WRITE_Q | FILL_DT, s->stream, nstep & 1);
 }
 
 cudaEvent_t pool_event(e2d_sim *s, size_t k) {
@@ -288,8 +304,13 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
       if (cudaMalloc(&s->U[k], sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
       if (cudaMemsetAsync(s->U[k], 0, sizeof(double) * 4 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
     }
-    if (cudaMalloc(&s->Q, sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
-    if (cudaMemsetAsync(s->Q, 0, sizeof(double) * 4 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+    for (int k = 0; k < 2; ++k) {
+      if (cudaMalloc(&s->Q[k], sizeof(double) * 4 * n) != cudaSuccess) return fail(E2D_ENOMEM);
+      if (cudaMemsetAsync(s->Q[k], 0, sizeof(double) * 4 * n, s->stream) != cudaSuccess) return fail(E2D_ECUDA);
+    }
+    s->q_tma = encode_q_map(&s->QTM[0], s->Q[0], s->kp) && encode_q_map(&s->QTM[1], s->Q[1], s->kp);
+    if (!s->q_tma) std::memset(s->QTM, 0, sizeof(s->QTM));
+    if (const char *v = std::getenv("E2D_F64_SPLIT")) s->f64_split = std::atoi(v) != 0;
   }
   if (cudaMalloc(&s->partial, sizeof(double) * reduce_partial_count(s->kp.g)) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&s->red_out, sizeof(double) * 8) != cudaSuccess) return fail(E2D_ENOMEM);
@@ -312,7 +333,8 @@ int e2d_destroy(e2d_sim *s) {
     if (s->U[k]) cudaFree(s->U[k]);
     if (s->W[k]) cudaFree(s->W[k]);
   }
-  if (s->Q) cudaFree(s->Q);
+  for (int k = 0; k < 2; ++k)
+    if (s->Q[k]) cudaFree(s->Q[k]);
   if (s->stage) cudaFree(s->stage);
   if (s->partial) cudaFree(s->partial);
   if (s->red_out) cudaFree(s->red_out);
@@ -397,16 +419,15 @@ int e2d_get_state(e2d_sim *s, int which, double *host, int layout) {
   return E2D_OK;
 }
 
-int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
-  if (!s || !filename || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad save_vtk args");
-  const e2d_params &p = s->p;
-  std::vector<double> host(4 * cells(s));
-  int rc = e2d_get_state(s, which, host.data(), E2D_LAYOUT_LEFT);
-  if (rc != E2D_OK) return rc;
+int e2d_write_vtk(const e2d_params *pin, const double *host, int layout, const char *filename) {
+  if (!pin || !host || !filename) return E2D_EINVAL;
+  if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return E2D_EINVAL;
+  const e2d_params &p = *pin;
+  if (p.isize != p.nx + 4 || p.jsize != p.ny + 4 || p.nx < 1 || p.ny < 1) return E2D_EINVAL;
   FILE *f = std::fopen(filename, "w");
-  if (!f) return set_err(s, E2D_EIO, std::string("cannot open ") + filename);
-  // text layout of src/HydroRun.h:557-607; numbers in the default ostream
-  // format (%g, 6 significant digits)
+  if (!f) return E2D_EIO;
+  // text layout of src/HydroRun.h:546-607; numbers in the default ostream
+  // format, which is printf's %g (6 significant digits)
   static const char *names[4] = {"rho", "E", "mx", "my"};
   const int one = 1;
   const bool big = (*(const char *)&one) == 0;
@@ -420,14 +441,28 @@ int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
   const size_t plane = (size_t)p.isize * p.jsize;
   for (int v = 0; v < 4; ++v) {
     std::fprintf(f, "    <DataArray type=\"Float64\" Name=\"%s\" format=\"ascii\" >\n", names[v]);
+    // interior cells, i fastest (the reference's LayoutLeft index order)
     for (int j = 2; j <= p.jsize - 3; ++j)
-      for (int i = 2; i <= p.isize - 3; ++i) std::fprintf(f, "%g ", host[i + (size_t)p.isize * j + plane * v]);
+      for (int i = 2; i <= p.isize - 3; ++i) {
+        const size_t k = layout == E2D_LAYOUT_LEFT ? i + (size_t)p.isize * j + plane * v
+                                                   : ((size_t)i * p.jsize + j) * 4 + v;
+        std::fprintf(f, "%g ", host[k]);
+      }
     std::fprintf(f, "\n    </DataArray>\n");
   }
   std::fprintf(f, "    </CellData>\n  </Piece>\n  </ImageData>\n</VTKFile>\n");
   const bool ok = std::ferror(f) == 0;
-  std::fclose(f);
-  return ok ? E2D_OK : set_err(s, E2D_EIO, std::string("write failed: ") + filename);
+  return (std::fclose(f) == 0 && ok) ? E2D_OK : E2D_EIO;
+}
+
+int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
+  if (!s || !filename || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad save_vtk args");
+  std::vector<double> host(4 * cells(s));
+  int rc = e2d_get_state(s, which, host.data(), E2D_LAYOUT_LEFT);
+  if (rc != E2D_OK) return rc;
+  rc = e2d_write_vtk(&s->p, host.data(), E2D_LAYOUT_LEFT, filename);
+  if (rc == E2D_EIO) return set_err(s, E2D_EIO, std::string("cannot write ") + filename);
+  return rc;
 }
 
 int e2d_make_boundaries(e2d_sim *s, int which) {
@@ -466,8 +501,8 @@ int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   }
   double *in = s->U[par], *out = s->U[par ^ 1];
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT;
-  E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk, mode, s->stream), "godunov primitives");
-  E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 0, dt,
+  E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q[0], s->clk, mode, s->stream), "godunov primitives");
+  E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q[0], in, out, s->clk, 0, dt,
                                    nullptr, s->stream), "godunov fluxes");
   return E2D_OK;
 }
@@ -487,12 +522,21 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   *s->clk_host = c;
   E2D_CK(s, cudaMemcpyAsync(s->clk, s->clk_host, sizeof(DevClock), cudaMemcpyHostToDevice, s->stream), "clock upload");
   const int par0 = (*nStep % 2 == 0) ? 0 : 1;
-  // FP32C: the first step's CFL maximum; later steps fold it in their epilogue
+  // FP32C and the fused FP64 step: the first step's CFL maximum (and the
+  // primitives of the input state); later steps fold it in their epilogue
   if (s->fp32) E2D_CK(s, launch_f32c_dt(s->kp32, s->W[par0], s->clk, *nStep & 1, s->stream), "initial dt");
   if (s->profiling) {
     size_t ev = 0;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     const std::string rs = riemann_name(s->p.riemannSolverType);
+    if (!s->fp32 && !s->f64_split) {
+      cudaEvent_t a = pool_event(s, ev++), b = pool_event(s, ev++);
+      if (!a || !b) return set_err(s, E2D_ECUDA, "event create");
+      E2D_CK(s, cudaEventRecord(a, s->stream), "event");
+      E2D_CK(s, enqueue_prologue(s, par0, *nStep), "prologue");
+      E2D_CK(s, cudaEventRecord(b, s->stream), "event");
+      marks.push_back({"k_fill_f64 (prologue)", {a, b}});
+    }
     for (int k = 0; k < n; ++k) {
       const int par = (par0 + k) & 1;
       cudaEvent_t a = pool_event(s, ev++), b = pool_event(s, ev++), c2 = pool_event(s, ev++);
@@ -505,13 +549,20 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
         marks.push_back({"k_step_f32c<" + rs + ">", {a, b}});
         continue;
       }
+      if (!s->f64_split) {
+        E2D_CK(s, cudaEventRecord(a, s->stream), "event");
+        E2D_CK(s, enqueue_step(s, par), "step");
+        E2D_CK(s, cudaEventRecord(b, s->stream), "event");
+        marks.push_back({"k_step_f64<" + rs + ">", {a, b}});
+        continue;
+      }
       double *in = s->U[par], *out = s->U[par ^ 1];
       E2D_CK(s, cudaEventRecord(a, s->stream), "event");
-      E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q, s->clk,
+      E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q[0], s->clk,
                                 FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT | FILL_DEVICE_CLOCK,
                                 s->stream), "fill");
       E2D_CK(s, cudaEventRecord(b, s->stream), "event");
-      E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q, in, out, s->clk, 1, 0.0,
+      E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q[0], in, out, s->clk, 1, 0.0,
                                        s->dt_trace, s->stream), "flux");
       E2D_CK(s, cudaEventRecord(c2, s->stream), "event");
       marks.push_back({"k_fill_f64", {a, b}});
@@ -524,6 +575,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
       record_kernel(s, m.first, ms);
     }
   } else {
+    E2D_CK(s, enqueue_prologue(s, par0, *nStep), "prologue");
     int done = 0;
     while (n - done >= kGraphSteps) {
       cudaGraphExec_t g;
@@ -542,7 +594,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   *t = s->clk_host->t;
   *nStep = s->clk_host->nstep;
   if (s->clk_host->status & E2D_FLAG_TIMEOUT)
-    return set_err(s, E2D_ETIMEOUT, "a row-staging wait gave up: the state of this call is incomplete");
+    return set_err(s, E2D_ETIMEOUT, "a staging wait gave up: the state of this call is incomplete");
   if (s->clk_host->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT))
     return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
                                                                               : "non-positive or non-finite dt");

@@ -1,16 +1,31 @@
 // e2d_config.cpp -- the reference's parameter contract on the host:
-// an ini reader with ConfigMap semantics (config/ConfigMap.{h,cpp},
-// config/inih/{ini,INIReader}.cpp) and HydroParams::setup / init
+// an ini reader with the reading rules of the reference's ConfigMap
+// (config/ConfigMap.{h,cpp} over config/inih) and HydroParams::setup / init
 // (src/HydroParams.cpp:42-190) filling the flat e2d_params of include/e2d.h.
 //
-// The behaviours that change numbers are kept on purpose:
+// Reading rules, each of which changes parsed values (restated from the
+// behaviour of config/inih/ini.cpp:66-150 and config/inih/INIReader.cpp):
+//  R1 the file is consumed in records of at most 199 bytes: a record ends
+//     after a '\n' or once 199 bytes are read (a longer line continues as the
+//     next record); records are numbered from 1; a NUL byte ends a record's text;
+//  R2 each record is trimmed of whitespace (isspace) at both ends;
+//  R3 a record that began with whitespace and is not blank, read while a key
+//     is current, replaces that key's value (no comment rule applies to it);
+//  R4 a record starting with ';' or '#' is a comment;
+//  R5 '[' opens a section name closed by the first ']'; a ';' right after a
+//     whitespace character ends the search (no ']': an error); the name
+//     keeps at most 49 bytes; afterwards no key is current;
+//  R6 any other record is name '=' value, split at the first '=' met before
+//     a whitespace-preceded ';' (none: an error); the name is right-trimmed,
+//     the value left-trimmed, cut at its first whitespace-preceded ';' and
+//     right-trimmed; the key becomes current, its name kept to 49 bytes;
+//  R7 keys are "section.name" lower-cased; a later value replaces an earlier;
+//  R8 parsing always reads to the end; the result is 0 or the number of the
+//     first record in error;
+// and, for values:
 //  - reals are parsed with strtof and returned as float, so gamma0=1.4 is
 //    really (double)1.4f (config/ConfigMap.cpp:31-40), defaults included;
-//  - integers use strtol base 0 ("010" is 8; config/inih/INIReader.cpp:57-66);
-//  - keys are "section.name" lower-cased (config/inih/INIReader.cpp:92-100);
-//  - lines are read in 200-byte pieces, ';'/'#' start comments, an inline ';'
-//    after whitespace ends a value, and an indented line continues (replaces)
-//    the previous key's value (config/inih/ini.cpp:66-150).
+//  - integers use strtol base 0 ("010" is 8; config/inih/INIReader.cpp:57-66).
 #include "e2d_internal.h"
 
 #include <cctype>
@@ -20,91 +35,104 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <vector>
 
 namespace e2d {
 
 namespace {
 
-constexpr int kMaxLine = 200;
-constexpr int kMaxSection = 50;
-constexpr int kMaxName = 50;
+constexpr size_t kRecordBytes = 199;  // R1
+constexpr size_t kNameBytes = 49;     // R5, R6
 
-char *rstrip(char *s) {
-  char *p = s + std::strlen(s);
-  while (p > s && std::isspace(static_cast<unsigned char>(*--p))) *p = '\0';
-  return s;
-}
+bool is_ws(char c) { return std::isspace(static_cast<unsigned char>(c)) != 0; }
 
-char *lskip(char *s) {
-  while (*s && std::isspace(static_cast<unsigned char>(*s))) s++;
-  return s;
-}
-
-// First occurrence of c, or of a ';' that follows whitespace, or the end.
-char *find_char_or_comment(char *s, char c) {
-  bool was_space = false;
-  while (*s && *s != c && !(was_space && *s == ';')) {
-    was_space = std::isspace(static_cast<unsigned char>(*s)) != 0;
-    s++;
+// R5/R6: index of the first `stop` in text[from, to), or of a ';' whose
+// preceding character (within the scanned range) is whitespace, else `to`.
+size_t scan(const std::string &text, size_t from, size_t to, char stop) {
+  for (size_t k = from; k < to; ++k) {
+    if (text[k] == stop) return k;
+    if (text[k] == ';' && k > from && is_ws(text[k - 1])) return k;
   }
-  return s;
+  return to;
 }
 
-void copy_bounded(char *dst, const char *src, size_t size) {
-  std::strncpy(dst, src, size);
-  dst[size - 1] = '\0';
+size_t trim_right(const std::string &text, size_t from, size_t to) {
+  while (to > from && is_ws(text[to - 1])) --to;
+  return to;
 }
 
-std::string make_key(const std::string &section, const std::string &name) {
+std::string make_key(const std::string &section, const std::string &name) {  // R7
   std::string key = section + "." + name;
   for (auto &ch : key) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
   return key;
 }
 
+// R1: the records of a file.
+bool read_records(const char *path, std::vector<std::string> *records) {
+  FILE *f = std::fopen(path, "rb");
+  if (!f) return false;
+  std::string rec;
+  int ch;
+  while ((ch = std::fgetc(f)) != EOF) {
+    rec.push_back(static_cast<char>(ch));
+    if (ch == '\n' || rec.size() == kRecordBytes) {
+      records->push_back(rec);
+      rec.clear();
+    }
+  }
+  if (!rec.empty()) records->push_back(rec);
+  std::fclose(f);
+  for (auto &r : *records) {
+    const size_t nul = r.find('\0');
+    if (nul != std::string::npos) r.resize(nul);
+  }
+  return true;
+}
+
 }  // namespace
 
 int IniMap::parse(const char *path) {
-  FILE *f = std::fopen(path, "r");
-  if (!f) return -1;
-  char line[kMaxLine];
-  char section[kMaxSection] = "";
-  char prev_name[kMaxName] = "";
-  int lineno = 0, error = 0;
-  while (std::fgets(line, sizeof(line), f) != nullptr) {
-    lineno++;
-    char *start = lskip(rstrip(line));
-    if (*prev_name && *start && start > line) {
-      // indented non-blank line: a new value for the previous key
-      values_[make_key(section, prev_name)] = start;
-    } else if (*start == ';' || *start == '#') {
-      // comment line
-    } else if (*start == '[') {
-      char *end = find_char_or_comment(start + 1, ']');
-      if (*end == ']') {
-        *end = '\0';
-        copy_bounded(section, start + 1, sizeof(section));
-        *prev_name = '\0';
-      } else if (!error) {
-        error = lineno;
+  std::vector<std::string> records;
+  if (!read_records(path, &records)) return -1;
+  std::string section, current;  // current: name of the key R3 continues
+  int first_error = 0;
+  auto fail = [&](int number) {
+    if (!first_error) first_error = number;
+  };
+  for (size_t r = 0; r < records.size(); ++r) {
+    const std::string &text = records[r];
+    const int number = static_cast<int>(r) + 1;
+    const size_t end = trim_right(text, 0, text.size());  // R2
+    size_t begin = 0;
+    while (begin < end && is_ws(text[begin])) ++begin;
+    if (begin == end) continue;  // blank
+    const char lead = text[begin];
+    if (begin > 0 && !current.empty()) {  // R3
+      values_[make_key(section, current)] = text.substr(begin, end - begin);
+    } else if (lead == ';' || lead == '#') {  // R4
+    } else if (lead == '[') {  // R5
+      const size_t close = scan(text, begin + 1, end, ']');
+      if (close < end && text[close] == ']') {
+        section = text.substr(begin + 1, std::min(close - begin - 1, kNameBytes));
+        current.clear();
+      } else {
+        fail(number);
       }
-    } else if (*start && *start != ';') {
-      char *end = find_char_or_comment(start, '=');
-      if (*end == '=') {
-        *end = '\0';
-        char *name = rstrip(start);
-        char *value = lskip(end + 1);
-        end = find_char_or_comment(value, '\0');
-        if (*end == ';') *end = '\0';
-        rstrip(value);
-        copy_bounded(prev_name, name, sizeof(prev_name));
-        values_[make_key(section, name)] = value;
-      } else if (!error) {
-        error = lineno;
+    } else {  // R6
+      const size_t eq = scan(text, begin, end, '=');
+      if (eq < end && text[eq] == '=') {
+        const std::string name = text.substr(begin, trim_right(text, begin, eq) - begin);
+        size_t vb = eq + 1;
+        while (vb < end && is_ws(text[vb])) ++vb;
+        const size_t ve = trim_right(text, vb, scan(text, vb, end, '\0'));
+        values_[make_key(section, name)] = text.substr(vb, ve - vb);
+        current = name.substr(0, kNameBytes);
+      } else {
+        fail(number);
       }
     }
   }
-  std::fclose(f);
-  return error;
+  return first_error;  // R8
 }
 
 std::string IniMap::get_string(const std::string &section, const std::string &name,

@@ -2,7 +2,10 @@
 // bit-identical to the reference (compiled with --fmad=false; every
 // expression keeps the reference's operation order).
 //
-// One time step is two launches:
+// The device time loop runs one fused launch per step (k_step_f64, after a
+// prologue k_fill_f64 that folds the first step's CFL maximum and writes the
+// primitives of the initial state).  The host-driven godunov_unsplit and the
+// batches run the same step as two launches:
 //   k_fill_f64         ghost fill (make_boundaries, src/HydroRun.h:388-399)
 //                      into both states, primitives of every cell
 //                      (ConvertToPrimitivesFunctor, src/HydroRunFunctors.h:84-143)
@@ -19,6 +22,9 @@
 #include "e2d_common.cuh"
 #include "e2d_f64_exact.cuh"
 #include "e2d_internal.h"
+#include "e2d_tma.cuh"
+
+#include <cudaTypedefs.h>
 
 #include <cstdint>
 
@@ -40,6 +46,13 @@ constexpr int FILL_BX = 64, FILL_BY = 4;
 template <int TX, int TY>
 constexpr size_t flux_smem_bytes() {
   return sizeof(double) * (4 * (TY + 4) * (TX + 4) + 2 * (4 * TY * (TX + 2)) + 2 * (4 * (TY + 2) * TX));
+}
+
+// The fused step's shared memory: the same tile + alignment slack of the
+// TMA destination.
+template <int TX, int TY>
+constexpr size_t step_smem_bytes() {
+  return flux_smem_bytes<TX, TY>() + 128;
 }
 
 __device__ __forceinline__ int src_lo_hi(int i, int n, int bc_lo, int bc_hi, bool &flip) {
@@ -226,7 +239,8 @@ __device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const doub
 // HLL flux (Harten, Lax, van Leer; Toro, "Riemann Solvers and Numerical
 // Methods for Fluid Dynamics", 3rd ed., eq. 10.21).  The reference declares
 // RIEMANN_HLL but has no solver; this uses riemann_hllc's cut-offs and Davis
-// wave speeds.  Operation order matches the oracle's riemann_hll.
+// wave speeds; the star flux multiplies by one reciprocal of SR - SL.
+// Operation order matches the oracle's riemann_hll.
 __device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const double *ql,
                                             const double *qr, double *flux) {
   const double rl = max_pos(ql[E2D_ID], ph.smallr);
@@ -265,10 +279,11 @@ __device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const doubl
 #pragma unroll
     for (int v = 0; v < 4; ++v) flux[v] = FR[v];
   } else {
+    // one division: the four star fluxes share the factor 1 / (SR - SL)
     const double sls = SL * SR;
-    const double den = SR - SL;
+    const double rden = 1.0 / (SR - SL);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) / den;
+    for (int v = 0; v < 4; ++v) flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) * rden;
   }
 }
 
@@ -284,6 +299,26 @@ __device__ __forceinline__ void riemann(const KPhys<double> &ph, const double *q
 }
 
 // ------------------------------------------------------------ kernel 1
+// CFL wave-speed term of a cell from its primitives (src/HydroRunFunctors.h:56-72):
+// (c + |u|) / dx + (c + |v|) / dy, c = sqrt(gamma p / d); a division by a
+// power-of-two dx, dy is the exact product by its reciprocal.
+__device__ __forceinline__ double cfl_term(const KPhys<double> &ph, double dd, double p, double ux, double uy) {
+  const double c = sqrt(ph.gamma0 * p / dd);
+  const double vx = c + fabs(ux);
+  const double vy = c + fabs(uy);
+  const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
+  const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
+  return tx + ty;
+}
+
+// E2D_FLAG_* bits of a cell's conserved values.
+__device__ __forceinline__ unsigned int state_flags(double rho, double e, double mx, double my) {
+  unsigned int f = 0;
+  if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) f |= E2D_FLAG_NONFINITE;
+  if (!(rho > 0.0)) f |= E2D_FLAG_DENSITY;
+  return f;
+}
+
 // Ghost fill + primitives + CFL term of array cell (i, j) (see the file
 // comment); `term`/`flags` receive its CFL term and E2D_FLAG_* bits.
 __device__ __forceinline__ void fill_cell(const KParams64 &kp, double *__restrict__ u_in,
@@ -329,16 +364,8 @@ __device__ __forceinline__ void fill_cell(const KParams64 &kp, double *__restric
       q[d + 3 * g.plane] = uy;
     }
     if ((mode & FILL_DT) && !ghost) {
-      // src/HydroRunFunctors.h:56-72
-      const double c = sqrt(ph.gamma0 * p / dd);
-      const double vx = c + fabs(ux);
-      const double vy = c + fabs(uy);
-      // vx / dx + vy / dy, as a product when the divisor is a power of two
-      const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
-      const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
-      term = tx + ty;
-      if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) flags |= E2D_FLAG_NONFINITE;
-      if (!(rho > 0.0)) flags |= E2D_FLAG_DENSITY;
+      term = cfl_term(ph, dd, p, ux, uy);
+      flags |= state_flags(rho, e, mx, my);
     }
   }
 }
@@ -373,13 +400,14 @@ __device__ __forceinline__ void fill_reduce(double term, unsigned int flags, uns
 
 __global__ void __launch_bounds__(FILL_BX *FILL_BY)
     k_fill_f64(const KParams64 kp, double *__restrict__ u_in, double *__restrict__ u_out,
-               double *__restrict__ q, DevClock *clk, const int mode) {
+               double *__restrict__ q, DevClock *clk, const int mode, const int acc_slot) {
   if ((mode & FILL_DEVICE_CLOCK) && !(clk->t < clk->t_end)) return;
   double term = 0.0;
   unsigned int flags = 0;
   fill_cell(kp, u_in, u_out, q, mode, blockIdx.x * FILL_BX + threadIdx.x, blockIdx.y * FILL_BY + threadIdx.y,
             term, flags);
-  if (mode & FILL_DT) fill_reduce(term, flags, &clk->invdt_bits, &clk->status);
+  if (mode & FILL_DT)
+    fill_reduce(term, flags, acc_slot < 0 ? &clk->invdt_bits : &clk->acc[acc_slot & 1], &clk->status);
 }
 
 // ------------------------------------------------------------ kernel 2
@@ -398,31 +426,32 @@ __device__ __forceinline__ double step_dt(const KPhys<double> &ph, unsigned long
   return dt;
 }
 
-// Stages 1-4 of the step for tile (bx, by) of a grid, block-wide; the
-// caller provides dt/dx, dt/dy and TX x TY shared memory.
-template <int RS, int TX, int TY, int NT>
-__device__ __forceinline__ void flux_tile(const KParams64 &kp, const double *__restrict__ q,
-                                          const double *__restrict__ u_in, double *__restrict__ u_out,
-                                          const int bx, const int by, const double dtdx, const double dtdy,
-                                          double *smem) {
-  constexpr int QW = TX + 4;  // primitives tile width (2-cell halo)
-  constexpr int QH = TY + 4;
-  constexpr int XW = TX + 2;  // x-face states: cells x in [-1, TX]
-  constexpr int YH = TY + 2;  // y-face states: cells y in [-1, TY]
-  double *sQ = smem;                   // [4][QH][QW]  primitives with halo
-  double *sXm = sQ + 4 * QH * QW;      // [4][TY][XW]  XMIN states, then x-fluxes
-  double *sXp = sXm + 4 * TY * XW;     // [4][TY][XW]  XMAX states
-  double *sYm = sXp + 4 * TY * XW;     // [4][YH][TX]  YMIN states, then y-fluxes
-  double *sYp = sYm + 4 * YH * TX;     // [4][YH][TX]  YMAX states
-  const KGeom &g = kp.g;
-  const KPhys<double> &ph = kp.ph;
-  const int tid = threadIdx.x;
+// Shared memory of a tile: primitives with a 2-cell halo, then the face
+// states (the scaled fluxes replace the XMIN / YMIN states in stage 3).
+template <int TX, int TY>
+struct TileSmem {
+  static constexpr int QW = TX + 4;  // primitives tile width (2-cell halo)
+  static constexpr int QH = TY + 4;
+  static constexpr int XW = TX + 2;  // x-face states: cells x in [-1, TX]
+  static constexpr int YH = TY + 2;  // y-face states: cells y in [-1, TY]
+  double *sQ, *sXm, *sXp, *sYm, *sYp;
+  __device__ explicit TileSmem(double *smem) {
+    sQ = smem;                   // [4][QH][QW]  primitives with halo
+    sXm = sQ + 4 * QH * QW;      // [4][TY][XW]  XMIN states, then x-fluxes
+    sXp = sXm + 4 * TY * XW;     // [4][TY][XW]  XMAX states
+    sYm = sXp + 4 * TY * XW;     // [4][YH][TX]  YMIN states, then y-fluxes
+    sYp = sYm + 4 * YH * TX;     // [4][YH][TX]  YMAX states
+  }
+};
 
-  const int i0 = bx * TX;  // array column of the tile's first halo cell
-  const int j0 = by * TY;
-
-  // stage 1: primitives of the tile and its 2-cell halo
-  for (int k = tid; k < QH * QW; k += NT) {
+// Stage 1 of the two-launch step: primitives of the tile and its 2-cell
+// halo from the primitives array (ghost cells included, written by the fill
+// kernel); cells beyond the array get a harmless 1.0.
+template <int TX, int TY, int NT>
+__device__ __forceinline__ void load_qtile(const KGeom &g, const double *__restrict__ q, int i0, int j0,
+                                           double *sQ) {
+  constexpr int QW = TX + 4, QH = TY + 4;
+  for (int k = threadIdx.x; k < QH * QW; k += NT) {
     const int y = k / QW, x = k - y * QW;
     const int gi = i0 + x, gj = j0 + y;
     if (gi < g.isize && gj < g.jsize) {
@@ -434,10 +463,55 @@ __device__ __forceinline__ void flux_tile(const KParams64 &kp, const double *__r
       for (int v = 0; v < 4; ++v) sQ[v * QH * QW + k] = 1.0;
     }
   }
-  __syncthreads();
+}
 
-  // stage 2: slopes, trace sources and face states of the tile cells and of
-  // the 1-cell ring (corners excluded) -- src/HydroBaseFunctor.h:214-291
+// Stage 1 of the fused step for tiles whose halo reaches ghost cells: the
+// primitives of a ghost cell are those of its source cell with the normal
+// velocity negated where the boundary reflects -- bit for bit the
+// primitives of the reference's ghost-filled state (u = mx / d changes only
+// its sign with mx; e, p and c depend on u^2).  Only interior cells of q are
+// read.
+template <int TX, int TY, int NT>
+__device__ __forceinline__ void gather_qtile(const KGeom &g, const double *__restrict__ q, int i0, int j0,
+                                             double *sQ) {
+  constexpr int QW = TX + 4, QH = TY + 4;
+  for (int k = threadIdx.x; k < QH * QW; k += NT) {
+    const int y = k / QW, x = k - y * QW;
+    const int gi = i0 + x, gj = j0 + y;
+    if (gi < g.isize && gj < g.jsize) {
+      bool fu, fv;
+      const int si = src_lo_hi(gi, g.nx, g.bc_xmin, g.bc_xmax, fu);
+      const int sj = src_lo_hi(gj, g.ny, g.bc_ymin, g.bc_ymax, fv);
+      const size_t s = (size_t)si + (size_t)g.isize * sj;
+      const double ux = q[s + 2 * g.plane], uy = q[s + 3 * g.plane];
+      sQ[k] = q[s];
+      sQ[QH * QW + k] = q[s + g.plane];
+      sQ[2 * QH * QW + k] = fu ? -ux : ux;
+      sQ[3 * QH * QW + k] = fv ? -uy : uy;
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sQ[v * QH * QW + k] = 1.0;
+    }
+  }
+}
+
+// Stages 2 and 3 of a tile whose primitives are in shared memory (the
+// caller has synchronised after writing them): slopes, trace sources and
+// face states of the tile cells and of the 1-cell ring (corners excluded)
+// -- src/HydroBaseFunctor.h:214-291 --, then one Riemann solve per face.
+// On return (after a block barrier) sXm holds the x-fluxes scaled by dt/dx
+// and sYm the y-fluxes scaled by dt/dy.
+template <int RS, int TX, int TY, int NT>
+__device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const double dtdx, const double dtdy,
+                                            double *smem) {
+  using T = TileSmem<TX, TY>;
+  constexpr int QW = T::QW, QH = T::QH, XW = T::XW, YH = T::YH;
+  const T sm(smem);
+  const double *sQ = sm.sQ;
+  double *sXm = sm.sXm, *sXp = sm.sXp, *sYm = sm.sYm, *sYp = sm.sYp;
+  const int tid = threadIdx.x;
+
+  // stage 2: slopes, trace sources and face states
   const int st_kind = (ph.slope_type == 2.0) ? 2 : (ph.slope_type == 1.0) ? 1 : 0;
   for (int k = tid; k < YH * XW; k += NT) {
     const int yy = k / XW, xx = k - yy * XW;  // cell (xx-1, yy-1) of the tile
@@ -515,26 +589,44 @@ __device__ __forceinline__ void flux_tile(const KParams64 &kp, const double *__r
     }
   }
   __syncthreads();
+}
 
-  // stage 4: conservative update in the reference's order
-  // (src/HydroRunFunctors.h:691-713): +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
-  for (int k = tid; k < TX * TY; k += NT) {
+// The conservative update of cell (x, y) of a tile in the reference's order
+// (src/HydroRunFunctors.h:691-713): +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1).
+template <int TX, int TY>
+__device__ __forceinline__ double update_var(const TileSmem<TX, TY> &sm, int v, int x, int y, double uu) {
+  using T = TileSmem<TX, TY>;
+  uu = uu + sm.sXm[v * TY * T::XW + y * T::XW + x + 1];
+  uu = uu - sm.sXm[v * TY * T::XW + y * T::XW + x + 2];
+  uu = uu + sm.sYm[v * T::YH * TX + (y + 1) * TX + x];
+  uu = uu - sm.sYm[v * T::YH * TX + (y + 2) * TX + x];
+  return uu;
+}
+
+// Stages 1-4 of the two-launch step for tile (bx, by) of a grid,
+// block-wide; the caller provides dt/dx, dt/dy and TX x TY shared memory.
+template <int RS, int TX, int TY, int NT>
+__device__ __forceinline__ void flux_tile(const KParams64 &kp, const double *__restrict__ q,
+                                          const double *__restrict__ u_in, double *__restrict__ u_out,
+                                          const int bx, const int by, const double dtdx, const double dtdy,
+                                          double *smem) {
+  const KGeom &g = kp.g;
+  const int i0 = bx * TX;  // array column of the tile's first halo cell
+  const int j0 = by * TY;
+  load_qtile<TX, TY, NT>(g, q, i0, j0, smem);
+  __syncthreads();
+  tile_fluxes<RS, TX, TY, NT>(kp.ph, dtdx, dtdy, smem);
+  const TileSmem<TX, TY> sm(smem);
+  // stage 4: conservative update
+  for (int k = threadIdx.x; k < TX * TY; k += NT) {
     const int y = k / TX, x = k - y * TX;
     const int gi = i0 + 2 + x, gj = j0 + 2 + y;
     if (gi < g.nx + 2 && gj < g.ny + 2) {
       const size_t s = (size_t)gi + (size_t)g.isize * gj;
 #pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        double uu = u_in[s + v * g.plane];
-        uu = uu + sXm[v * TY * XW + y * XW + x + 1];
-        uu = uu - sXm[v * TY * XW + y * XW + x + 2];
-        uu = uu + sYm[v * YH * TX + (y + 1) * TX + x];
-        uu = uu - sYm[v * YH * TX + (y + 2) * TX + x];
-        u_out[s + v * g.plane] = uu;
-      }
+      for (int v = 0; v < 4; ++v) u_out[s + v * g.plane] = update_var<TX, TY>(sm, v, x, y, u_in[s + v * g.plane]);
     }
   }
-
 }
 
 template <int RS, int TX, int TY, int NT, int MINB>
@@ -584,6 +676,190 @@ __global__ void __launch_bounds__(NT, MINB)
       clk->t = clk->t + dt;  // only this block writes t during the step
       clk->nstep = ns + 1;
       clk->invdt_bits = 0ull;
+      clk->done_blocks = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// ------------------------------------------------------------ the fused step
+// Block maximum of the CFL term into *acc and the OR of the flags into
+// *status, one atomic of each per block (fmax drops NaN like the reference's
+// reducer; positive doubles order like their bit patterns).
+template <int NT>
+__device__ __forceinline__ void block_fold(double term, unsigned int flags, unsigned long long *acc,
+                                           unsigned int *status) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) term = fmax(term, __shfl_xor_sync(0xffffffffu, term, off));
+  flags = __reduce_or_sync(0xffffffffu, flags);
+  __shared__ double wmax[NT / 32];
+  __shared__ unsigned int wflags[NT / 32];
+  const int tid = threadIdx.x;
+  if ((tid & 31) == 0) {
+    wmax[tid >> 5] = term;
+    wflags[tid >> 5] = flags;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double m = wmax[0];
+    unsigned int f = wflags[0];
+#pragma unroll
+    for (int w = 1; w < NT / 32; ++w) {
+      m = fmax(m, wmax[w]);
+      f |= wflags[w];
+    }
+    if (m > 0.0) atomicMax(acc, (unsigned long long)__double_as_longlong(m));
+    if (f) atomicOr(status, f);
+  }
+}
+
+template <int TX, int TY>
+__host__ __device__ constexpr unsigned int qtile_bytes() {
+  return (unsigned int)(sizeof(double) * 4 * (TX + 4) * (TY + 4));
+}
+
+// One whole time step of the device loop (src/main.cpp:128-143 around
+// godunov_unsplit_impl, src/HydroRun.h:279-364), one TX x TY tile per block:
+//  - dt from the CFL maximum of the input state, clock->acc[nstep & 1],
+//    which the previous step (or the prologue fill) folded;
+//  - stage 1: primitives of the tile and its 2-cell halo, from q_in (the
+//    primitives of u_in's interior cells): one TMA copy of the box for tiles
+//    whose halo is interior, else a gather through the boundary map;
+//  - stages 2-3: slopes, trace, face states, one Riemann solve per face;
+//  - epilogue: the conservative update into u_out, the primitives of the
+//    new cells into q_out and their CFL term, folded into
+//    clock->acc[(nstep + 1) & 1] with one atomic per block;
+//  - boundary tiles write the ghost fill of u_in into the ghost cells of
+//    both states (make_boundaries + deep_copy of the reference), reading
+//    only interior cells of u_in, which no block writes;
+//  - the last block to finish advances the loop state.
+// Bit-identical to the two-launch step; FP64 work per cell is the same.
+template <int RS, int TX, int TY, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    k_step_f64(const KParams64 kp, const __grid_constant__ CUtensorMap tm_q, const int use_tma,
+               const double *__restrict__ q_in, double *__restrict__ q_out, double *__restrict__ u_in,
+               double *__restrict__ u_out, DevClock *clk, double *__restrict__ dt_trace) {
+  extern __shared__ unsigned char smem_raw[];
+  // a TMA destination must be 128-byte aligned
+  double *smem = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+  __shared__ double s_dt[3];
+  __shared__ int s_run, s_par;
+  __shared__ __align__(8) unsigned long long s_bar;
+  const KGeom &g = kp.g;
+  const KPhys<double> &ph = kp.ph;
+  const int tid = threadIdx.x;
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int i0 = bx * TX, j0 = by * TY;  // array cell of the halo box's corner
+  constexpr int QW = TX + 4, QH = TY + 4;
+  const bool tma_tile = use_tma && i0 >= 2 && j0 >= 2 && i0 + QW <= g.nx + 2 && j0 + QH <= g.ny + 2;
+  if (tid == 0) {
+    const int run = clk->t < clk->t_end;
+    const int par = clk->nstep & 1;
+    const double dt = step_dt(ph, clk->acc[par], clk->t, clk->t_end);
+    s_dt[0] = dt;
+    s_dt[1] = dt / ph.dx;
+    s_dt[2] = dt / ph.dy;
+    s_run = run;
+    s_par = par;
+    if (run && tma_tile) {
+      mbar_init(&s_bar, 1u);
+      mbar_init_fence();
+      // wait_test: tile (1, 1) never copies, so its bounded wait runs out
+      if (!(kp.wait_test && bx == 1 && by == 1)) {
+        mbar_arrive_expect(&s_bar, qtile_bytes<TX, TY>());
+        tma_load_3d(smem, &tm_q, i0, j0, 0, &s_bar);
+      }
+    }
+  }
+  __syncthreads();
+  if (!s_run) return;  // past t_end: no copy was issued
+  const int par = s_par;
+  bool ok = true;
+  if (tma_tile) {
+    ok = __syncthreads_and(mbar_wait(&s_bar, 0u));
+    if (!ok) {
+      // flag the step, then wait (bounded) for the copy that may still land
+      // in this block's shared memory before leaving the tile
+      if (tid == 0) atomicOr(&clk->status, E2D_FLAG_TIMEOUT);
+      mbar_wait(&s_bar, 0u);
+      __syncthreads();
+    }
+  } else {
+    gather_qtile<TX, TY, NT>(g, q_in, i0, j0, smem);
+    __syncthreads();
+  }
+
+  double term = 0.0;
+  unsigned int flags = 0;
+  if (ok) {
+    tile_fluxes<RS, TX, TY, NT>(ph, s_dt[1], s_dt[2], smem);
+    const TileSmem<TX, TY> sm(smem);
+    for (int k = tid; k < TX * TY; k += NT) {
+      const int y = k / TX, x = k - y * TX;
+      const int gi = i0 + 2 + x, gj = j0 + 2 + y;
+      if (gi < g.nx + 2 && gj < g.ny + 2) {
+        const size_t s = (size_t)gi + (size_t)g.isize * gj;
+        double un[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          un[v] = update_var<TX, TY>(sm, v, x, y, u_in[s + v * g.plane]);
+          u_out[s + v * g.plane] = un[v];
+        }
+        double dd, p, ux, uy;
+        primitives(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy);
+        q_out[s] = dd;
+        q_out[s + g.plane] = p;
+        q_out[s + 2 * g.plane] = ux;
+        q_out[s + 3 * g.plane] = uy;
+        term = fmax(term, cfl_term(ph, dd, p, ux, uy));
+        flags |= state_flags(un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV]);
+      }
+    }
+  }
+
+  // ghost cells next to this tile: those whose nearest interior cell is in it
+  const bool lo_x = bx == 0, hi_x = bx == (int)gridDim.x - 1;
+  const bool lo_y = by == 0, hi_y = by == (int)gridDim.y - 1;
+  if (lo_x || hi_x || lo_y || hi_y) {
+    const int xa = lo_x ? 0 : i0 + 2, xb = hi_x ? g.isize : i0 + 2 + TX;
+    const int ya = lo_y ? 0 : j0 + 2, yb = hi_y ? g.jsize : j0 + 2 + TY;
+    const int w = xb - xa, n = w * (yb - ya);
+    for (int k = tid; k < n; k += NT) {
+      const int j = ya + k / w, i = xa + k % w;
+      if (i >= 2 && i < g.nx + 2 && j >= 2 && j < g.ny + 2) continue;
+      bool fu, fv;
+      const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
+      const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
+      const size_t s = (size_t)si + (size_t)g.isize * sj, d = (size_t)i + (size_t)g.isize * j;
+      double v4[4] = {u_in[s], u_in[s + g.plane], u_in[s + 2 * g.plane], u_in[s + 3 * g.plane]};
+      if (fu) v4[E2D_IU] = -v4[E2D_IU];
+      if (fv) v4[E2D_IV] = -v4[E2D_IV];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        u_in[d + v * g.plane] = v4[v];
+        u_out[d + v * g.plane] = v4[v];
+      }
+    }
+  }
+
+  block_fold<NT>(term, flags, &clk->acc[par ^ 1], &clk->status);
+
+  // the last block to finish advances the loop state (src/main.cpp:139-143)
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned int ticket = atomicAdd(&clk->done_blocks, 1u);
+    if (ticket == gridDim.x * gridDim.y - 1) {
+      __threadfence();
+      const double dt = s_dt[0];
+      const int ns = clk->nstep;
+      const int slot = ns - clk->trace_base;
+      if (dt_trace && slot >= 0 && slot < clk->trace_cap) dt_trace[slot] = dt;
+      if (!(dt > 0.0) || nonfinite(dt)) clk->status |= E2D_FLAG_BAD_DT;
+      clk->dt = dt;
+      clk->t = clk->t + dt;  // only this block writes t during the step
+      clk->nstep = ns + 1;
+      clk->acc[par] = 0ull;  // read by this step; folded into by the next
       clk->done_blocks = 0u;
       __threadfence();
     }
@@ -800,10 +1076,10 @@ __global__ void k_init_f64(const KParams64 kp, const e2d_params p, double *__res
 
 
 cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, double *q,
-                            DevClock *clk, int mode, cudaStream_t s) {
+                            DevClock *clk, int mode, cudaStream_t s, int acc_slot) {
   dim3 block(FILL_BX, FILL_BY);
   dim3 grid((kp.g.isize + FILL_BX - 1) / FILL_BX, (kp.g.jsize + FILL_BY - 1) / FILL_BY);
-  k_fill_f64<<<grid, block, 0, s>>>(kp, u_in, u_out, q, clk, mode);
+  k_fill_f64<<<grid, block, 0, s>>>(kp, u_in, u_out, q, clk, mode, acc_slot);
   return cudaGetLastError();
 }
 
@@ -832,10 +1108,20 @@ static cudaError_t set_flux_smem() {
                               (int)flux_smem_bytes<TX, TY>());
 }
 
+template <int RS, int TX, int TY, int NT, int MINB>
+static cudaError_t set_step_smem() {
+  return cudaFuncSetAttribute(k_step_f64<RS, TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)step_smem_bytes<TX, TY>());
+}
+
 template <int RS>
 static cudaError_t configure_rs() {
   cudaError_t e = set_flux_smem<RS, 32, 32, 512, 1>();
   if (e == cudaSuccess) e = set_flux_smem<RS, 32, 16, 256, 2>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 32, 512, 1>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 16, 256, 2>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 31, 512, 1>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 15, 256, 2>();
   return e;
 }
 
@@ -893,6 +1179,70 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
     default:
       return launch_flux_t<E2D_RIEMANN_APPROX>(kp, q, u_in, u_out, clk, use_clock, host_dt, dt_trace, s);
   }
+}
+
+// Fused-step tile shapes (kp.tile): 0 -> 32 x 32 cells, 512 threads, one
+// block per SM; 1 -> 32 x 16, 256 threads, two blocks per SM; 2 -> 32 x 31
+// (2047 Riemann solves: four full rounds of 512 threads); 3 -> 32 x 15 (two
+// blocks per SM, 1007 solves: four rounds of 256).  Results do not depend on
+// the shape.
+template <int RS, int TX, int TY, int NT, int MINB>
+static cudaError_t launch_step_shape(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
+                                     double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
+                                     cudaStream_t s) {
+  dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
+  k_step_f64<RS, TX, TY, NT, MINB><<<grid, NT, step_smem_bytes<TX, TY>(), s>>>(kp, tm_q, use_tma, q_in, q_out, u_in,
+                                                                                u_out, clk, dt_trace);
+  return cudaGetLastError();
+}
+
+template <int RS>
+static cudaError_t launch_step_t(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
+                                 double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
+                                 cudaStream_t s) {
+  switch (kp.tile) {
+    case 1: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    case 2: return launch_step_shape<RS, 32, 31, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    case 3: return launch_step_shape<RS, 32, 15, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    default: return launch_step_shape<RS, 32, 32, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+  }
+}
+
+cudaError_t launch_step_f64(const KParams64 &kp, int riemann, const CUtensorMap &tm_q, int use_tma,
+                            const double *q_in, double *q_out, double *u_in, double *u_out, DevClock *clk,
+                            double *dt_trace, cudaStream_t s) {
+  switch (riemann) {
+    case E2D_RIEMANN_HLLC:
+      return launch_step_t<E2D_RIEMANN_HLLC>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    case E2D_RIEMANN_HLL:
+      return launch_step_t<E2D_RIEMANN_HLL>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    default:
+      return launch_step_t<E2D_RIEMANN_APPROX>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+  }
+}
+
+// The box of the fused step's primitives tile for the tile shape of kp:
+// dimensions (isize, jsize, 4 planes), box (TX + 4) x (TY + 4) x 4.  Row and
+// plane strides must be multiples of 16 bytes, so isize must be even; false
+// (tiles are then gathered) otherwise or if the driver cannot encode it.
+bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult qr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr) != cudaSuccess ||
+        qr != cudaDriverEntryPointSuccess)
+      return nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode || (kp.g.isize & 1) || (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
+  const int ty = kp.tile == 1 ? 16 : kp.tile == 2 ? 31 : kp.tile == 3 ? 15 : 32;
+  const cuuint64_t dims[3] = {(cuuint64_t)kp.g.isize, (cuuint64_t)kp.g.jsize, 4};
+  const cuuint64_t strides[2] = {(cuuint64_t)kp.g.isize * sizeof(double), (cuuint64_t)kp.g.plane * sizeof(double)};
+  const cuuint32_t box[3] = {32 + 4, (cuuint32_t)ty + 4, 4};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double *>(q), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 cudaError_t launch_eval_f64(const KParams64 &kp, int what, int n, const double *in, double *out,

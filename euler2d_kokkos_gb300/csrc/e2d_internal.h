@@ -57,7 +57,9 @@ struct KPhys {
 struct KParams64 {
   KGeom g;
   KPhys<double> ph;
-  int tile;  // flux kernel tile shape (see k_flux_update_f64)
+  int tile;       // flux / fused step kernel tile shape (see launch_step_f64)
+  int wait_test;  // nonzero: tile (1, 1) of the fused step never stages its primitives,
+                  // so its bounded wait runs out (E2D_TEST_WAIT_TIMEOUT=1; tests the timeout path)
 };
 
 // FP32 step with FP64 copies of the constants the exact dt recompute uses.
@@ -88,8 +90,9 @@ struct DevClock {
   unsigned int done_blocks;       // blocks of the current step kernel that finished
   unsigned int status;            // E2D_FLAG_* bits seen by the device
   unsigned int fill_count;        // blocks of the current primitives kernel that finished
-  // FP32 path: the step of parity n reads the CFL maximum of its input from
-  // acc[n & 1] and folds that of its output into acc[(n + 1) & 1]
+  // FP32 path and the fused FP64 step: the step of parity n reads the CFL
+  // maximum of its input from acc[n & 1] and folds that of its output into
+  // acc[(n + 1) & 1]
   unsigned long long acc[2];
   double *trace;  // FP32 path: device dt trace (trace_cap entries) or null
 };
@@ -98,7 +101,8 @@ enum : unsigned int {
   E2D_FLAG_NONFINITE = 1u,  // a state value is NaN or Inf
   E2D_FLAG_DENSITY = 2u,    // a density <= 0 was clamped to smallr
   E2D_FLAG_BAD_DT = 4u,     // the CFL wave-speed maximum is not a finite positive number
-  E2D_FLAG_TIMEOUT = 8u,    // a bounded device wait (row staging) gave up; that strip is not updated
+  E2D_FLAG_TIMEOUT = 8u,    // a bounded device wait (row or tile staging) gave up; that strip or tile
+                            // is not updated
 };
 
 // Modes of the primitives kernel.
@@ -106,13 +110,23 @@ enum : int {
   FILL_WRITE_Q = 1,          // store primitives of every cell
   FILL_GHOSTS_IN = 2,        // store the ghost fill into the input state (make_boundaries)
   FILL_GHOSTS_OUT = 4,       // store the ghost fill into the output state (deep_copy)
-  FILL_DT = 8,               // fold the CFL term of interior cells into clock->invdt_bits
+  FILL_DT = 8,               // fold the CFL term of interior cells into clock->invdt_bits (or acc[slot])
   FILL_DEVICE_CLOCK = 16,    // do nothing once clock->t >= clock->t_end
 };
 
 // FP64 kernels (e2d_fp64.cu, bit-identical to the reference).
+// acc_slot < 0: FILL_DT folds into clk->invdt_bits, else into clk->acc[acc_slot & 1].
 cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, double *q,
-                            DevClock *clk, int mode, cudaStream_t s);
+                            DevClock *clk, int mode, cudaStream_t s, int acc_slot = -1);
+// One fused step of the device time loop: reads u_in and q_in (primitives of
+// u_in's interior, tm_q its TMA map when use_tma) and clk->acc[nstep & 1];
+// writes u_out, the ghost cells of both states, q_out and clk->acc[(nstep+1) & 1].
+cudaError_t launch_step_f64(const KParams64 &kp, int riemann, const CUtensorMap &tm_q, int use_tma,
+                            const double *q_in, double *q_out, double *u_in, double *u_out, DevClock *clk,
+                            double *dt_trace, cudaStream_t s);
+// TMA map of a primitives array for the fused step's tile shape; false if
+// isize is odd or the driver cannot encode it (tiles are gathered then).
+bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp);
 // use_clock = 1: dt from clk (src/main.cpp:128-134 on the device) and the
 // loop bookkeeping; 0: the caller's host_dt, clock untouched.
 cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const double *q,

@@ -41,7 +41,10 @@ class RunStats:
     tuning: tuple = ()
     failed: list = field(default_factory=list)     # indices of solves stopped for good
     escalated: list = field(default_factory=list)  # indices of FP32C solves re-run in FP64
+    rejected: list = field(default_factory=list)   # indices of requests larger than the whole pool
     wasted_cell_updates: int = 0                   # updates of stopped solves (not in cell_updates)
+    states: dict = field(default_factory=dict)     # serve(keep=...): index -> final state
+    peak_live: int = 0                             # most solves on the GPU at once
 
     @property
     def gcell_per_s(self) -> float:
@@ -131,6 +134,7 @@ def run_batched(solves, pool_bytes=64 << 30, iters_per_call=16, autotune=True, k
             if not tuned:
                 b.autotune(2)
                 tuned = True
+            stats.peak_live = max(stats.peak_live, len(live))
             b.run(iters_per_call)
             stats.iterations += iters_per_call
             for i in list(live):
@@ -201,10 +205,13 @@ def run_one_at_a_time(solves, chunk=256, on_nonfinite="fp64"):
 
 
 def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, autotune=True,
-          time_limit_s=None, on_nonfinite="fp64"):
+          time_limit_s=None, on_nonfinite="fp64", keep=None):
     """Open-loop Poisson arrivals (rate_per_s) of `solves` in order; returns
     RunStats with per-request latencies and the aggregate throughput over
-    the makespan.  on_nonfinite: "fp64" or "drop" (module doc)."""
+    the makespan.  on_nonfinite: "fp64" or "drop" (module doc).  keep:
+    optional set of indices whose final states are returned in
+    RunStats.states.  A request that does not fit even the empty pool is
+    recorded in RunStats.rejected and never admitted."""
     rng = np.random.default_rng(seed)
     arrivals = np.cumsum(rng.exponential(1.0 / rate_per_s, size=len(solves)))
     stats = RunStats()
@@ -230,7 +237,12 @@ def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, au
                 except E2DError as e:
                     if e.status != 2:
                         raise
-                    break  # no room: wait for completions
+                    if live:
+                        break  # no room: wait for completions
+                    # the pool is empty and still too small: it never fits
+                    stats.rejected.append(k)
+                    queue.pop(0)
+                    continue
                 live[i] = (k, arr)
                 queue.pop(0)
             if not live:
@@ -241,11 +253,16 @@ def serve(solves, rate_per_s, pool_bytes=150 << 30, iters_per_call=8, seed=1, au
             if not tuned and len(live) >= 4:
                 b.autotune(2)
                 tuned = True
+            stats.peak_live = max(stats.peak_live, len(live))
             b.run(iters_per_call)
             stats.iterations += iters_per_call
             done_t = time.perf_counter() - t0
             for i in list(live):
                 k, arr = live[i]
+                if keep is not None and k in keep:
+                    _, _, active, ok = b.poll(i)
+                    if ok and not active:
+                        stats.states[k] = b.get_state(i)
                 r = reaper.reap(b, i, k)
                 if r is None:
                     continue

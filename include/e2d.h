@@ -148,6 +148,10 @@ int e2d_get_state(e2d_sim *sim, int which, double *host, int layout);
  * or U2 (1) and an ASCII VTK ImageData (.vti) file of the interior cells,
  * variables rho, E, mx, my in the reference's text format. */
 int e2d_save_vtk(e2d_sim *sim, int which, const char *filename);
+/* The text writer of HydroRun::saveVTK (src/HydroRun.h:546-607) for a state
+ * already on the host: p->nx x p->ny interior cells of `host` (LayoutLeft or
+ * LayoutRight FP64, ghosts included) into `filename`.  No device work. */
+int e2d_write_vtk(const e2d_params *p, const double *host, int layout, const char *filename);
 /* Device address of U (which = 0) or U2 (1), LayoutLeft FP64, for zero-copy
  * use.  FP32C handles return a converted copy (hi + lo, ghosts filled) in a
  * staging array that the next call on the handle may overwrite. */
@@ -302,6 +306,13 @@ enum {
 };
 int e2d_eval_device(const e2d_params *p, int what, int n, const double *in, double *out, double dtdx,
                     double dtdy);
+
+/* Measured throughput of this GPU's FP64 operations in G operations/s:
+ * rates[0..5] = fused multiply-add, add, multiply, divide, square root,
+ * maximum (8 independent chains per thread, 8 blocks of 256 threads per SM,
+ * CUDA events).  No counterpart in the reference: it is the denominator of
+ * the FP64-pipe roofline that bounds the FP64 step on GB300. */
+int e2d_fp64_rates(double rates[6]);
 
 /* Per-kernel device time: with profiling on, e2d_step_n launches kernels
  * directly with CUDA events around each one.  names/ms/launches receive, per

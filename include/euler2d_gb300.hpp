@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -42,10 +43,39 @@ inline void check(int status, const char *what, const e2d_sim *sim = nullptr) {
 
 // ConfigMap: holds the ini path; values are read by HydroParams::setup with
 // the reference's ConfigMap semantics (strtof reals, case-insensitive keys).
+// The getters are ConfigMap's / INIReader's (config/ConfigMap.h:25-47,
+// config/inih/INIReader.h): strings, strtol base-0 integers, strtof reals,
+// 1/yes/true/on and 0/no/false/off booleans, defaults for absent keys.
 class ConfigMap {
  public:
   explicit ConfigMap(std::string filename) : filename_(std::move(filename)) {}
   const std::string &filename() const { return filename_; }
+  std::string getString(const std::string &section, const std::string &name,
+                        const std::string &default_value) const {
+    std::vector<char> buf(4096);
+    if (e2d_ini_get_string(filename_.c_str(), section.c_str(), name.c_str(), default_value.c_str(),
+                           buf.data(), buf.size()) != E2D_OK)
+      return default_value;
+    return std::string(buf.data());
+  }
+  long getInteger(const std::string &section, const std::string &name, long default_value) const {
+    const std::string v = getString(section, name, "");
+    char *end = nullptr;
+    const long n = std::strtol(v.c_str(), &end, 0);
+    return end > v.c_str() ? n : default_value;
+  }
+  float getFloat(const std::string &section, const std::string &name, float default_value) const {
+    const std::string v = getString(section, name, "");
+    char *end = nullptr;
+    const float x = std::strtof(v.c_str(), &end);
+    return end > v.c_str() ? x : default_value;
+  }
+  bool getBool(const std::string &section, const std::string &name, bool default_value) const {
+    const std::string v = getString(section, name, "");
+    if (v == "1" || v == "yes" || v == "true" || v == "on") return true;
+    if (v == "0" || v == "no" || v == "false" || v == "off") return false;
+    return default_value;
+  }
 
  private:
   std::string filename_;
@@ -137,6 +167,19 @@ class HydroRun {
     Uhost.resize(Udata.size());
     check(e2d_get_state(sim_, Udata.which, Uhost.data(), E2D_LAYOUT_LEFT), "copy_to_host", sim_);
     return Uhost;
+  }
+  // src/HydroRun.h:486-495 (saveData; VTK only, HDF5 is not built) and
+  // :506-609 (saveVTK): Udata as <outputDir>/<outputPrefix>_<iStep, 7
+  // digits>.vti, the names read from the ini's [output] section.
+  void saveData(const DataArray &Udata, int iStep, const std::string &name) {
+    if (params.ioVTK) saveVTK(Udata, iStep, name);
+  }
+  void saveVTK(const DataArray &Udata, int iStep, const std::string & /*name*/) {
+    char num[16];
+    std::snprintf(num, sizeof(num), "%07d", iStep);
+    const std::string fn = configMap.getString("output", "outputDir", "./") + "/" +
+                           configMap.getString("output", "outputPrefix", "output") + "_" + num + ".vti";
+    check(e2d_save_vtk(sim_, Udata.which, fn.c_str()), "saveVTK", sim_);
   }
   void copy_from_host(const DataArray &Udata, const std::vector<double> &host) {
     check(e2d_set_state(sim_, Udata.which, host.data(), E2D_LAYOUT_LEFT), "copy_from_host", sim_);

@@ -293,9 +293,9 @@ static void riemann_hll(const orc_params *p, const double ql[4], const double qr
     for (int v = 0; v < 4; ++v) flux[v] = FR[v];
   } else {
     double sls = SL * SR;
-    double den = SR - SL;
+    double rden = 1.0 / (SR - SL); /* one division shared by the four fluxes */
     for (int v = 0; v < 4; ++v)
-      flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) / den;
+      flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) * rden;
   }
 }
 

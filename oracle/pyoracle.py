@@ -224,6 +224,7 @@ class ReferenceLib:
                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
         L.ref_initial_state.argtypes = [ctypes.c_char_p, dp]
         L.ref_make_boundaries.argtypes = [ctypes.c_char_p, dp]
+        L.ref_save_vtk.argtypes = [ctypes.c_char_p, dp, ctypes.c_int]
         L.ref_compute_dt.argtypes = [ctypes.c_char_p, dp]
         L.ref_compute_dt.restype = ctypes.c_double
         L.ref_primitives.argtypes = [ctypes.c_char_p, ctypes.c_int, dp, dp, dp]
@@ -283,6 +284,11 @@ class ReferenceLib:
         u = np.array(u, dtype=np.float64, order="C", copy=True)
         self.L.ref_make_boundaries(ini.encode(), _ptr(u))
         return u
+
+    def save_vtk(self, ini: str, u, istep: int):
+        """HydroRun::saveData(U, istep) of the reference on state u: the .vti
+        file named by the ini's [output] outputDir and outputPrefix."""
+        self.L.ref_save_vtk(ini.encode(), _ptr(np.ascontiguousarray(u, dtype=np.float64)), int(istep))
 
     def compute_dt(self, ini: str, u):
         return self.L.ref_compute_dt(ini.encode(), _ptr(np.ascontiguousarray(u)))

@@ -182,6 +182,21 @@ extern "C"
     return 0;
   }
 
+  // HydroRun::saveData -> saveVTK (src/HydroRun.h:486-609) of a
+  // caller-supplied state: writes <outputDir>/<outputPrefix>_<iStep, 7
+  // digits>.vti as the ini's [output] section names it.
+  int
+  ref_save_vtk(const char * ini, const double * u, int iStep)
+  {
+    ConfigMap   cm{ std::string(ini) };
+    HydroParams params;
+    params.setup(cm);
+    HydroRun<Dev> hydro(params, cm);
+    to_real(hydro.U.data(), u, (long)params.isize * params.jsize * 4);
+    hydro.saveData(hydro.U, iStep, "U");
+    return 0;
+  }
+
   // make_boundaries (src/HydroRun.h:388-399) applied in place to u.
   int
   ref_make_boundaries(const char * ini, double * u)

@@ -16,6 +16,8 @@ Outputs (small, committed):
     sedov.npz     the Sedov post-processing (src/main.cpp:175-179) of a 64x64
                   point blast after 60 steps: the .npy files the reference's
                   ComputeRadialProfileFunctor writes, for three ring counts
+    vtk.npz       HydroRun::saveVTK output: the .vti bytes of a 32x24 state
+                  and the SHA-256 of the .vti of the C1 state
 
     python tests/golden/make_golden.py --only sedov   regenerates one file
 """
@@ -74,6 +76,16 @@ implementationVersion=1.9
                                  cfl=0.5, xmax=0.445, ymax=0.089,
                                  extra="[shocked_bubble]\nbubble_pressure=1.0132\n"),
     "bad_impl": C.ini_text(16, 16, extra="[OTHER]\nimplementationVersion=7\n"),
+    # every reading rule at once: a value continued on an indented line, a
+    # line longer than 199 bytes (its tail read as a continuation), inline
+    # ';' with and without whitespace before it, a line without '=', a
+    # section header whose ']' follows a comment, tab separators
+    "quirks": ("[run]\ntEnd=3.5\nnStepmax=77\n[mesh]\nnx=20\nny=10\n   30\n"
+               "xmin=" + " " * 194 + "  -0.5\n"
+               "xmax=2.0 ;comment\nymax=1.5;x\nymin=;0.25\n"
+               "[hydro]\ngamma0=1.3\nthis line has no equals sign\ncfl = 0.3\n"
+               "slope_type\t=\t1.0\t; tab comment\n[hydro ;broken]\nriemann=hll\nproblem=blast\n"
+               "# comment\n; comment\nsmallr=1e-9\n\t\t2e-9\n[OTHER]\nimplementationVersion=1\n"),
 }
 
 
@@ -190,6 +202,34 @@ def gen_c1(R: ReferenceLib, tmp: str) -> dict:
             "l1_interior": [float(np.abs(interior[v]).sum()).hex() for v in range(4)]}
 
 
+VTK_SMALL_INI = C.ini_text(32, 24, problem="implode", gamma0=1.666, xmin=-1.0, xmax=1.0)
+
+
+def gen_vtk(R: ReferenceLib, tmp: str) -> dict:
+    """HydroRun::saveVTK of the reference: the .vti bytes of a 32x24
+    implosion on [-1,1]x[0,1] after 20 steps from its own initial condition
+    (state included), and the SHA-256 of the .vti of the 256^2 implosion
+    after 1000 steps (the C1 state)."""
+    out = {"small_ini": np.array(VTK_SMALL_INI)}
+    outdir = os.path.join(tmp, "vtk")
+    os.makedirs(outdir, exist_ok=True)
+    section = f"\n[output]\noutputDir={outdir}\noutputPrefix=ref\n"
+    path = C.write_ini(VTK_SMALL_INI + section, tmp, "vtk_small.ini")
+    u, _, _, ns = R.run(path, None, 20)
+    R.save_vtk(path, u, ns)
+    out["small_u"] = u
+    out["small_nsteps"] = np.array(ns)
+    out["small_vti"] = np.frombuffer(open(os.path.join(outdir, f"ref_{ns:07d}.vti"), "rb").read(), dtype=np.uint8)
+    text = C.ini_text(256, 256, problem="implode", nStepmax=1000)
+    path = C.write_ini(text + section, tmp, "vtk_c1.ini")
+    u, _, _, ns = R.run(path, C.implode_diag_state(256, 256, C.f32(1.4)), 1000)
+    R.save_vtk(path, u, ns)
+    vti = open(os.path.join(outdir, f"ref_{ns:07d}.vti"), "rb").read()
+    out["c1_vti_sha256"] = np.array(hashlib.sha256(vti).hexdigest())
+    out["c1_vti_bytes"] = np.array(len(vti))
+    return out
+
+
 def gen_sedov(R: ReferenceLib, tmp: str) -> dict:
     """The reference's own initial condition and 60 steps, then its radial
     profile with 7, 40 and 150 rings: the raw bytes of both .npy files."""
@@ -210,7 +250,7 @@ def main():
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["params", "kat", "runs", "c1", "sedov"])
+    ap.add_argument("--only", choices=["params", "kat", "runs", "c1", "sedov", "vtk"])
     only = ap.parse_args().only
     R = ReferenceLib()
     tmp = tempfile.mkdtemp(prefix="e2d_golden_")
@@ -224,6 +264,8 @@ def main():
     if only in (None, "c1"):
         with open(os.path.join(HERE, "c1.json"), "w") as f:
             json.dump(gen_c1(R, tmp), f, indent=1)
+    if only in (None, "vtk"):
+        np.savez_compressed(os.path.join(HERE, "vtk.npz"), **gen_vtk(R, tmp))
     if only in (None, "sedov"):
         np.savez_compressed(os.path.join(HERE, "sedov.npz"), **gen_sedov(R, tmp))
     print("golden fixtures written to", HERE)

@@ -48,7 +48,7 @@ REF_TO_FIELD = {
 }
 
 
-@pytest.mark.parametrize("name", ["plain", "formatting", "defaults", "shocked_bubble", "bad_impl"])
+@pytest.mark.parametrize("name", ["plain", "formatting", "defaults", "shocked_bubble", "bad_impl", "quirks"])
 def test_params_from_ini_match_reference(golden_dir, tmp_path, name):
     g = json.load(open(os.path.join(golden_dir, "params.json")))[name]
     path = C.write_ini(g["ini"], str(tmp_path), f"{name}.ini")
@@ -116,7 +116,7 @@ def test_make_params_matches_ini(tmp_path):
 
 def test_header_is_plain_c(tmp_path):
     """include/e2d.h compiles as C11 (the boundary cgo, JNI and ctypes
-    callers bind), and the loop of INTEGRATION.md's C example type-checks."""
+    callers bind), and a C driver loop over its entry points type-checks."""
     import shutil
     import subprocess
 

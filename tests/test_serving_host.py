@@ -110,3 +110,41 @@ def test_one_at_a_time_applies_the_same_policy(monkeypatch):
     assert st.solves == 0 and st.failed == [0, 1] and st.escalated == []
     st = serving.run_one_at_a_time(solves(e2d.PRECISION_FP64))
     assert st.solves == 2 and st.escalated == [] and st.wasted_cell_updates == 0
+
+
+class FullPoolBatch:
+    """e2d.Batch stand-in whose pool never has room: admit always raises
+    E2D_ENOMEM, as e2d_batch_admit does for a solve larger than the pool."""
+
+    def __init__(self, **kw):
+        self.admits = 0
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+    def admit(self, params, t_end, u0=None):
+        self.admits += 1
+        raise e2d.E2DError(2, "e2d_batch_admit")
+
+    def stats(self):
+        return (0, 0)
+
+
+def test_serve_rejects_a_request_the_empty_pool_cannot_hold(monkeypatch):
+    """With nothing live, E2D_ENOMEM means the request never fits: serve()
+    records it and goes on instead of waiting for completions that cannot
+    come (no time limit is given, so a wait would never end)."""
+    monkeypatch.setattr(serving, "Batch", FullPoolBatch)
+    sv = solves(e2d.PRECISION_FP32C)
+    st = serving.serve(sv, rate_per_s=1e6, autotune=False)
+    assert st.rejected == [0, 1] and st.solves == 0 and st.latencies == []
+
+
+def test_run_batched_raises_on_a_request_the_empty_pool_cannot_hold(monkeypatch):
+    monkeypatch.setattr(serving, "Batch", FullPoolBatch)
+    with pytest.raises(e2d.E2DError) as ei:
+        serving.run_batched(solves(e2d.PRECISION_FP32C), autotune=False)
+    assert ei.value.status == 2
