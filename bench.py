@@ -39,7 +39,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "Gcell-updates/s"
 HBM_FALLBACK_GBS = 6800.0
-BYTES_PER_CELL = {"fp64": 64, "fp32c": 64}  # read + write of the 4 conserved variables
+BYTES_PER_CELL = {"fp64": 64, "fp32c": 64, "fp64_fast": 64}  # read + write of the 4 conserved variables
 BLAST = dict(blast_radius=0.125, blast_center_x=0.5, blast_center_y=0.5, blast_density_in=1.0,
              blast_density_out=1.0, blast_pressure_in=10.0, blast_pressure_out=0.1)
 
@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32c", "fp64_fast"])
     ap.add_argument("--problem", default=None, choices=["blast", "four_quadrant"])
     ap.add_argument("--nx", type=int, default=None)
     ap.add_argument("--riemann", default="hllc", choices=["hllc", "hll", "approx"])
@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--c3-nx", type=int, default=8192, help="grid side of --mode c3")
     a = ap.parse_args()
     if a.problem is None:
-        a.problem = "blast" if a.precision == "fp64" else "four_quadrant"
+        a.problem = "four_quadrant" if a.precision == "fp32c" else "blast"
     if a.nx is None:
         a.nx = 4096 if a.problem == "blast" else 8192
     return a
@@ -84,7 +84,8 @@ def dist_env():
 
 
 def workload_params(e2d, problem, nx, riemann, precision):
-    prec = e2d.PRECISION_FP64 if precision == "fp64" else e2d.PRECISION_FP32C
+    prec = {"fp64": e2d.PRECISION_FP64, "fp32c": e2d.PRECISION_FP32C,
+            "fp64_fast": e2d.PRECISION_FP64_FAST}[precision]
     if problem == "blast":
         return e2d.make_params(nx, nx, problem="blast", riemann=riemann, gamma0=1.4, cfl=0.8,
                                slope_type=2.0, bc=(1, 1, 1, 1), precision=prec, **BLAST)
@@ -363,46 +364,57 @@ def roofline(kt, precision, cells, prefix):
 
 
 # FP64 operations of the fused FP64 step (k_step_f64 in
-# euler2d_kokkos_gb300/csrc/e2d_fp64.cu), counted from its source.  Adds,
-# subtracts and multiplies count 1 each (the FP64 pipe runs them at its FMA
-# rate); divisions and square roots are counted apart and weighted by their
-# measured cost (FMA rate / their rate); fmax and comparisons by theirs.
+# euler2d_kokkos_gb300/csrc/e2d_fp64.cu), counted from its source, by kind:
+# "addmul" (adds, subtracts, multiplies), "fma", "div", "sqrt" and "max"
+# (fmax and FP64 comparisons).  Each kind is weighted by its measured cost
+# in FMA-rate cycles (FMA rate / its rate: on GB300 adds and multiplies run
+# at ~0.84 of the FMA rate, a division or a square root costs ~9 FMAs).
 # Limiter min/max, sign tests, cut-offs against positive constants and the
 # exact scalings by 0.5 and 2 run on the integer pipe and are not counted.
 F64_OPS = {
     # stage 2, per cell of the tile and of its 1-cell ring: 8 limited slopes
     # (3 subtractions each, f64x::slope_limited) and the trace sources
-    # (trace_sources: 3 + 3 + 2 + 2 products, 3 + 3 + 2 + 2 sums less one
-    # shared dux + dvy; dpx / r and dpy / r)
-    "slopes_trace": {"simple": 24 + 20, "div": 2},
+    # (trace_sources: 10 products and 10 sums; dpx / r and dpy / r)
+    "slopes_trace": {"addmul": 24 + 20, "div": 2},
     # face_pair for the 4 variables of one direction: s0 * dtd, then
     # q - h + sx and q + h + sx
-    "faces_dir": {"simple": 4 * 5},
+    "faces_dir": {"addmul": 4 * 5},
     # stage 3, one solve plus the 4 products by dt/dx
-    "hllc": {"simple": 51 + 4, "div": 6, "sqrt": 2},
-    "hll": {"simple": 64 + 4, "div": 3, "sqrt": 2},
+    "hllc": {"addmul": 51 + 4, "div": 6, "sqrt": 2},
+    "hll": {"addmul": 64 + 4, "div": 3, "sqrt": 2},
     # epilogue per cell: the update (4 x 4 sums), primitives (7 + 3
     # divisions), the CFL term (6 + a division and a square root), and
     # fmax / comparisons (the running maximum, the dx / dy power-of-two
     # tests, the density test, the block fold's shuffles, ~6)
-    "epilogue": {"simple": 16 + 7 + 6, "div": 3 + 1, "sqrt": 1, "max": 6},
+    "epilogue": {"addmul": 16 + 7 + 6, "div": 3 + 1, "sqrt": 1, "max": 6},
+}
+# The opt-in fast forms (precision fp64_fast, *_fast in e2d_fp64_blocks.cuh):
+# FMAs, and one reciprocal per denominator (rcp_nr: a hardware estimate on
+# the MUFU unit and two Newton steps, 4 FMAs) in place of the divisions.
+F64_OPS_FAST = {
+    "slopes_trace": {"addmul": 24 + 6, "fma": 12},
+    "faces_dir": {"fma": 4 * 3},
+    "hllc": {"addmul": 39, "fma": 27, "sqrt": 2},
+    "hll": {"addmul": 42, "fma": 26, "sqrt": 2},
+    "epilogue": {"addmul": 28, "fma": 7, "sqrt": 1, "max": 4},
 }
 F64_TILES = {0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}
 
 
-def fp64_ops_per_cell(riemann, tile=0):
+def fp64_ops_per_cell(riemann, tile=0, fast=False):
     """FP64 operations per cell-update of the fused step by kind, for a tile
     shape: per tile, (TX+2)(TY+2)-4 slope/trace evaluations, 2 TX TY + 2 TX
     + 2 TY face-pair directions, (TX+1) TY + TX (TY+1) solves and TX TY
     epilogues.  None for the iterative approx solver."""
-    if riemann not in F64_OPS:
+    ops = F64_OPS_FAST if fast else F64_OPS
+    if riemann not in ops:
         return None
-    tx, ty = F64_TILES.get(tile, (32, 32))
+    tx, ty = (32, 32) if fast else F64_TILES.get(tile, (32, 32))
     n = {"slopes_trace": (tx + 2) * (ty + 2) - 4, "faces_dir": 2 * tx * ty + 2 * tx + 2 * ty,
          riemann: (tx + 1) * ty + tx * (ty + 1), "epilogue": tx * ty}
-    tot = {"simple": 0.0, "div": 0.0, "sqrt": 0.0, "max": 0.0}
+    tot = {"addmul": 0.0, "fma": 0.0, "div": 0.0, "sqrt": 0.0, "max": 0.0}
     for part, cnt in n.items():
-        for kind, v in F64_OPS[part].items():
+        for kind, v in ops[part].items():
             tot[kind] += cnt * v / (tx * ty)
     return tot
 
@@ -410,7 +422,7 @@ def fp64_ops_per_cell(riemann, tile=0):
 _FP64_RATES = None
 
 
-def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0):
+def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0, fast=False):
     """FP64-pipe roofline of the fused step, live: the probe's measured rates
     (e2d_fp64_rates, this run), the source-counted operations per cell in FMA
     equivalents, and the fraction of the FMA peak the kernel sustained."""
@@ -418,16 +430,17 @@ def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0):
     if _FP64_RATES is None:
         _FP64_RATES = e2d.fp64_rates()
     r = _FP64_RATES
-    ops = fp64_ops_per_cell(riemann, tile)
+    ops = fp64_ops_per_cell(riemann, tile, fast)
     out = {"rates_gops": r, "peak_gops": r["fma"], "unit": "G FP64 FMA-equivalent ops/s",
            "peak_source": "e2d_fp64_rates probe in this run (8 chains/thread, 8x256 threads/SM, CUDA events)"}
     if not ops:
         return out
-    cost = {"simple": 1.0, "div": r["fma"] / r["div"], "sqrt": r["fma"] / r["sqrt"], "max": r["fma"] / r["max"]}
+    cost = {"fma": 1.0, "addmul": r["fma"] / min(r["add"], r["mul"]), "div": r["fma"] / r["div"],
+            "sqrt": r["fma"] / r["sqrt"], "max": r["fma"] / r["max"]}
     per_cell = sum(ops[k] * cost[k] for k in ops)
     achieved = per_cell * cells / (kernel_ms * 1e-3) / 1e9
     out.update({"ops_per_cell": ops, "fma_equivalent_per_cell": per_cell,
-                "cost_in_fma": {"div": cost["div"], "sqrt": cost["sqrt"], "max": cost["max"]},
+                "cost_in_fma": {k: cost[k] for k in ("addmul", "div", "sqrt", "max")},
                 "achieved_gops": achieved, "frac": achieved / r["fma"],
                 "ops_source": "counted from k_step_f64's source (bench.py F64_OPS)"})
     return out
@@ -455,17 +468,17 @@ def l1_check(e2d, nx, t_end, problem="four_quadrant"):
     return res
 
 
-def l1_steps(e2d, problem, nx, steps):
-    """FP32C vs FP64 (bit-identical to the reference) on the bench's own
-    workload: the same initial state advanced `steps` steps of the device time
-    loop at nx^2; relative L1 of density (FP64 accumulation) and the largest
-    relative difference of the dt sequences."""
+def l1_steps(e2d, problem, nx, steps, precs=("fp64", "fp32c")):
+    """FP32C (or another precision) vs FP64 (bit-identical to the reference)
+    on the bench's own workload: the same initial state advanced `steps`
+    steps of the device time loop at nx^2; relative L1 of density (FP64
+    accumulation) and the largest relative difference of the dt sequences."""
     out = {}
-    for prec in ("fp64", "fp32c"):
+    for prec in precs:
         h = e2d.HydroRun(workload_params(e2d, problem, nx, "hllc", prec))
         t, ns, tr = h.step_n(steps, 10.0, 0.0, 0)
         out[prec] = (h, t, ns, np.asarray(tr))
-    (h64, t64, n64, tr64), (h32, t32, n32, tr32) = out["fp64"], out["fp32c"]
+    (h64, t64, n64, tr64), (h32, t32, n32, tr32) = out[precs[0]], out[precs[1]]
     d, r = h32.l1_diff(n32 % 2, h64, n64 % 2, e2d.ID)  # on the device, FP64 sums
     h32.close()
     h64.close()
@@ -725,16 +738,18 @@ def main():
                 barrier, dist)
     value = cells * args.steps * world / (m["ms"] / 1e3) / 1e9
     kt = m["kernels"]
-    prefix = "k_step_f64" if args.precision == "fp64" else "k_step_f32c"
+    f64 = args.precision in ("fp64", "fp64_fast")
+    prefix = "k_step_f64" if f64 else "k_step_f32c"
     roof = roofline(kt, args.precision, cells, prefix)
-    if roof and args.precision == "fp64":
+    if roof and f64:
         roof["note"] = "the FP64 step is bound by GB300's FP64 pipe, not HBM: see fp64_pipe"
         roof["fp64_pipe"] = fp64_pipe_info(e2d, args.riemann, roof["kernel_ms_avg"], cells,
-                                           int(os.environ.get("E2D_F64_TILE", "0")))
+                                           int(os.environ.get("E2D_F64_TILE", "0")),
+                                           fast=args.precision == "fp64_fast")
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f32 (compensated hi/lo state, FP64 dt)",
+            "dtype": "f64" if f64 else "f32 (compensated hi/lo state, FP64 dt)",
             "data": "synthetic", "impl": "gb300",
             "config": config(args.problem, nx, args.riemann, args.precision),
             "ms_per_step_profiled": m["ms_profiled"] / args.steps,
@@ -743,7 +758,7 @@ def main():
             "gpu_launches": int(sum(v[1] for v in kt.values())),
             "reference_formula_mcell_per_s": (nx + 4) ** 2 * args.steps * world / (m["ms"] / 1e3) / 1e6}
 
-    if not args.no_secondary and args.precision == "fp64" and rank == 0:
+    if not args.no_secondary and args.precision == "fp64" and rank == 0:  # the default line
         # the FP32 compensated mode on the four-quadrant problem at 8192^2
         s = measure(e2d, torch, args, "fp32c", "four_quadrant", 8192, args.steps, args.warmup, local,
                     barrier, None, with_e2e=False, with_clocks=False)
@@ -784,6 +799,20 @@ def main():
             "ms_per_step": tl["ms"] / args.steps,
             "kernels": {k: {"ms_total": v[0], "launches": v[1]} for k, v in tl["kernels"].items()},
             "fused_over_two_launch": (tl["ms"] / m["ms"])}
+        # the opt-in fast FP64 forms (FMAs, shared reciprocals; not
+        # bit-identical) on the same workload, with their error against the
+        # bit-exact FP64 path on this grid after the same steps
+        fa = measure(e2d, torch, args, "fp64_fast", args.problem, nx, args.steps, args.warmup, local,
+                     barrier, None, with_e2e=False, with_clocks=False)
+        rf = roofline(fa["kernels"], "fp64_fast", cells, "k_step_f64")
+        if rf:
+            rf["fp64_pipe"] = fp64_pipe_info(e2d, args.riemann, rf["kernel_ms_avg"], cells, fast=True)
+        line["fp64_fast"] = {
+            "config": config(args.problem, nx, args.riemann, "fp64_fast"),
+            "value": cells * args.steps / (fa["ms"] / 1e3) / 1e9, "unit": METRIC,
+            "ms_per_step": fa["ms"] / args.steps, "roofline": rf,
+            "accuracy": l1_steps(e2d, args.problem, nx, args.steps, precs=("fp64", "fp64_fast")),
+            "tolerance": "dt within 1e-12 relative, relative L1 <= 1e-10 (tests/test_gpu_fp64_fast.py)"}
         # batched mixed solves against one at a time, and one loaded serving point
         line["batch"] = batch_summary(512, 24)
         line["batch_fp64"] = batch_summary(64, 8, fp64=True)

@@ -24,13 +24,13 @@ from . import build as _build
 
 __all__ = ["HydroParams", "HydroRun", "E2DError", "load_library", "ID", "IP", "IE", "IU", "IV",
            "RIEMANN", "BC_REFLECT", "BC_ABSORB", "BC_PERIODIC", "PROBLEMS", "PRECISION_FP64",
-           "PRECISION_FP32C"]
+           "PRECISION_FP32C", "PRECISION_FP64_FAST"]
 
 ID, IP, IE, IU, IV = 0, 1, 1, 2, 3
 RIEMANN = {"approx": 0, "hll": 1, "hllc": 2}
 BC_REFLECT, BC_ABSORB, BC_PERIODIC = 1, 2, 3
 PROBLEMS = {"implode": 0, "blast": 1, "four_quadrant": 2, "discontinuity": 3, "shocked_bubble": 4}
-PRECISION_FP64, PRECISION_FP32C = 0, 1
+PRECISION_FP64, PRECISION_FP32C, PRECISION_FP64_FAST = 0, 1, 2
 LAYOUT_LEFT, LAYOUT_RIGHT = 0, 1
 
 STATUS = {0: "E2D_OK", 1: "E2D_EINVAL", 2: "E2D_ENOMEM", 3: "E2D_ENUMERIC", 4: "E2D_ETIMEOUT",

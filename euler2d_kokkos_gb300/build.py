@@ -33,6 +33,7 @@ UNITS = [
     ("e2d_fp32c.cu", ["-use_fast_math"]),
     ("e2d_reduce.cu", ["--fmad=false"]),
     ("e2d_probe.cu", ["--fmad=false"]),
+    ("e2d_impl12.cu", ["--fmad=false"]),
     ("e2d_noalloc.cu", []),
     ("e2d_batch.cu", []),
     ("e2d_capi.cu", []),

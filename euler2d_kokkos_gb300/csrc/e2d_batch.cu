@@ -391,7 +391,7 @@ int e2d_batch_free_bytes(const e2d_batch *b, size_t *free_bytes, size_t *largest
 size_t e2d_batch_instance_bytes(const e2d_params *pin) {
   if (!pin) return 0;
   e2d_params p = *pin;
-  if (params_init(&p, nullptr) != E2D_OK) return 0;
+  if (params_init(&p, nullptr) != E2D_OK || p.precision == E2D_PRECISION_FP64_FAST) return 0;
   KParams32 kp;
   make_kparams32(p, &kp);
   if (p.precision == E2D_PRECISION_FP64) return PoolAllocator::round(inst_bytes64(kp.g));
@@ -404,6 +404,8 @@ int e2d_batch_admit(e2d_batch *b, const e2d_params *pin, double t_end, const dou
   int rc = params_init(&p, nullptr);
   if (rc != E2D_OK) return berr(b, rc, "admit: invalid parameters");
   if (p.riemannSolverType != b->riemann) return berr(b, E2D_EINVAL, "admit: riemann solver differs from the batch's");
+  if (p.precision == E2D_PRECISION_FP64_FAST)
+    return berr(b, E2D_EINVAL, "admit: fp64_fast runs on single simulations only (e2d_step_n)");
   int slot = -1;
   for (int k = 0; k < b->max_inst; ++k)
     if (!b->slots[k].used) {

@@ -27,6 +27,8 @@ struct e2d_sim {
   CUtensorMap QTM[2];                 // FP64: TMA maps of Q[0], Q[1] (fused step's tile staging)
   int q_tma = 0;                      // FP64: both maps encoded (isize even)
   int f64_split = 0;                  // FP64 device loop as two launches per step (E2D_F64_SPLIT=1)
+  int impl = 0;                       // FP64: implementationVersion (1, 2: the debug orchestrations)
+  double *impl_scratch = nullptr;     // FP64, implementation 1: stored slopes and fluxes
   float *W[2] = {nullptr, nullptr};   // FP32C: compensated U and U2 (8 float planes)
   CUtensorMap TM[2];                  // FP32C: TMA maps of W[0], W[1] (row staging)
   double *stage = nullptr;            // FP32C: FP64 staging array (set/get/init)
@@ -100,6 +102,9 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   };
   kp->ph.inv_dx_pow2 = inv_pow2(p.dx);
   kp->ph.inv_dy_pow2 = inv_pow2(p.dy);
+  kp->ph.inv_dx = 1.0 / p.dx;
+  kp->ph.inv_dy = 1.0 / p.dy;
+  kp->fast = p.precision == E2D_PRECISION_FP64_FAST ? 1 : 0;
   kp->tile = 0;
   if (const char *v = std::getenv("E2D_F64_TILE")) kp->tile = std::atoi(v);
   const char *wt = std::getenv("E2D_TEST_WAIT_TIMEOUT");
@@ -134,6 +139,13 @@ cudaError_t enqueue_step(e2d_sim *s, int par) {
     return launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 1,
                             0.0, s->stream);
   double *in = s->U[par], *out = s->U[par ^ 1];
+  if (s->impl != 0) {
+    const int m = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_COPY_OUT | FILL_DT | FILL_DEVICE_CLOCK;
+    cudaError_t e = launch_fill_f64(s->kp, in, out, s->Q[0], s->clk, m, s->stream);
+    if (e != cudaSuccess) return e;
+    return launch_impl12_f64(s->kp, s->impl, s->p.riemannSolverType, s->Q[0], out, s->impl_scratch, s->clk, 1,
+                             0.0, s->dt_trace, s->stream);
+  }
   if (!s->f64_split)
     return launch_step_f64(s->kp, s->p.riemannSolverType, s->QTM[par], s->q_tma, s->Q[par], s->Q[par ^ 1], in,
                            out, s->clk, s->dt_trace, s->stream);
@@ -147,7 +159,7 @@ cudaError_t enqueue_step(e2d_sim *s, int par) {
 // Before the fused FP64 steps of a device-loop call: the primitives of the
 // input state and its CFL maximum, which the first step reads.
 cudaError_t enqueue_prologue(e2d_sim *s, int par, int nstep) {
-  if (s->fp32 || s->f64_split) return cudaSuccess;
+  if (s->fp32 || s->f64_split || s->impl != 0) return cudaSuccess;
   return launch_fill_f64(s->kp, s->U[par], nullptr, s->Q[par], s->clk, FILL_WRITE_Q | FILL_DT, s->stream, nstep & 1);
 }
 
@@ -311,6 +323,14 @@ int e2d_create(const e2d_params *pin, e2d_sim **out) {
     s->q_tma = encode_q_map(&s->QTM[0], s->Q[0], s->kp) && encode_q_map(&s->QTM[1], s->Q[1], s->kp);
     if (!s->q_tma) std::memset(s->QTM, 0, sizeof(s->QTM));
     if (const char *v = std::getenv("E2D_F64_SPLIT")) s->f64_split = std::atoi(v) != 0;
+    s->impl = (p.implementationVersion == 1 || p.implementationVersion == 2) ? p.implementationVersion : 0;
+    if (s->kp.fast) {
+      // the fast forms exist in the fused step of implementation 0 only
+      if (s->impl != 0) return fail(E2D_EINVAL);
+      s->f64_split = 0;
+    }
+    if (const size_t k = impl12_scratch_doubles(s->kp, s->impl))
+      if (cudaMalloc(&s->impl_scratch, sizeof(double) * k) != cudaSuccess) return fail(E2D_ENOMEM);
   }
   if (cudaMalloc(&s->partial, sizeof(double) * reduce_partial_count(s->kp.g)) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&s->red_out, sizeof(double) * 8) != cudaSuccess) return fail(E2D_ENOMEM);
@@ -335,6 +355,7 @@ int e2d_destroy(e2d_sim *s) {
   }
   for (int k = 0; k < 2; ++k)
     if (s->Q[k]) cudaFree(s->Q[k]);
+  if (s->impl_scratch) cudaFree(s->impl_scratch);
   if (s->stage) cudaFree(s->stage);
   if (s->partial) cudaFree(s->partial);
   if (s->red_out) cudaFree(s->red_out);
@@ -493,6 +514,7 @@ int e2d_compute_dt(e2d_sim *s, int useU, double *dt) {
 
 int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   if (!s) return E2D_EINVAL;
+  if (s->kp.fast) return set_err(s, E2D_EINVAL, "fp64_fast runs through the device time loop (e2d_step_n) only");
   const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
   if (s->fp32) {
     E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 0, dt,
@@ -500,6 +522,13 @@ int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
     return E2D_OK;
   }
   double *in = s->U[par], *out = s->U[par ^ 1];
+  if (s->impl != 0) {  // src/HydroRun.h:332-360
+    E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q[0], s->clk, FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_COPY_OUT,
+                              s->stream), "godunov primitives");
+    E2D_CK(s, launch_impl12_f64(s->kp, s->impl, s->p.riemannSolverType, s->Q[0], out, s->impl_scratch, s->clk, 0,
+                                dt, nullptr, s->stream), "godunov implementation 1/2");
+    return E2D_OK;
+  }
   const int mode = FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT;
   E2D_CK(s, launch_fill_f64(s->kp, in, out, s->Q[0], s->clk, mode, s->stream), "godunov primitives");
   E2D_CK(s, launch_flux_update_f64(s->kp, s->p.riemannSolverType, s->Q[0], in, out, s->clk, 0, dt,
@@ -553,7 +582,8 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
         E2D_CK(s, cudaEventRecord(a, s->stream), "event");
         E2D_CK(s, enqueue_step(s, par), "step");
         E2D_CK(s, cudaEventRecord(b, s->stream), "event");
-        marks.push_back({"k_step_f64<" + rs + ">", {a, b}});
+        marks.push_back({s->impl ? "implementation " + std::to_string(s->impl) + " step<" + rs + ">"
+                                 : "k_step_f64<" + rs + ">", {a, b}});
         continue;
       }
       double *in = s->U[par], *out = s->U[par ^ 1];

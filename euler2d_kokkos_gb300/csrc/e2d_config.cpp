@@ -319,7 +319,8 @@ int params_from_ini(const IniMap &m, e2d_params *p, std::string *msg) {
       p->fq_state[q][v] = opt_float("four_quadrant", fq_names[v] + std::to_string(q), p->fq_state[q][v]);
   p->implode_shape = (int)m.get_integer("implode", "shape", 0);
   const std::string prec = m.get_string("gb300", "precision", "fp64");
-  p->precision = (prec == "fp32c") ? E2D_PRECISION_FP32C : E2D_PRECISION_FP64;
+  p->precision = (prec == "fp32c") ? E2D_PRECISION_FP32C
+                  : (prec == "fp64_fast") ? E2D_PRECISION_FP64_FAST : E2D_PRECISION_FP64;
 
   // getFloat then an implicit float->int conversion (:149-155)
   p->implementationVersion = (int)m.get_float("OTHER", "implementationVersion", 0.0f);
@@ -370,8 +371,9 @@ int params_init(e2d_params *p, std::string *msg) {
   if (!(p->dx > 0.0) || !(p->dy > 0.0)) return bad("xmax > xmin and ymax > ymin required");
   if (!(p->smallr > 0.0) || !(p->smallc > 0.0)) return bad("smallr and smallc must be > 0");
   if (p->riemannSolverType < 0 || p->riemannSolverType > 2) return bad("riemann solver must be 0, 1 or 2");
-  if (p->precision != E2D_PRECISION_FP64 && p->precision != E2D_PRECISION_FP32C)
-    return bad("precision must be fp64 or fp32c");
+  if (p->precision != E2D_PRECISION_FP64 && p->precision != E2D_PRECISION_FP32C &&
+      p->precision != E2D_PRECISION_FP64_FAST)
+    return bad("precision must be fp64, fp32c or fp64_fast");
   if (p->problemType < 0 || p->problemType > 4) return bad("problem must be 0..4");
   return E2D_OK;
 }

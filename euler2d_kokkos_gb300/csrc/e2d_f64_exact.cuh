@@ -28,7 +28,7 @@ __device__ __forceinline__ double from_bits(unsigned long long b) {
 
 // FP64 multiply kept out of line so that it runs only on the lanes that need
 // it (a branch, not a predicated instruction issued by the whole warp).
-__device__ __noinline__ double mul_slow(double a, double b) { return a * b; }
+static __device__ __noinline__ double mul_slow(double a, double b) { return a * b; }
 
 // fmax(x, c) for c > 0: non-negative doubles order like their bit patterns as
 // signed integers and every negative x (including -0) is below c.
@@ -76,7 +76,7 @@ __device__ __forceinline__ double twice(double x) {
   return mul_slow(2.0, x);
 }
 
-__device__ __noinline__ bool product_le0_slow(double a, double b) { return (a * b) <= 0.0; }
+static __device__ __noinline__ bool product_le0_slow(double a, double b) { return (a * b) <= 0.0; }
 
 // src/HydroBaseFunctor.h:421-455, one direction, for slope_type st in {1, 2}:
 //   dlft = st*(q-qm); drgt = st*(qp-q); dcen = 0.5*(qp-qm)

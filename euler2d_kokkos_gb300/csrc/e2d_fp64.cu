@@ -19,9 +19,7 @@
 //                      bookkeeping of src/main.cpp:128-143.
 // The reference evaluates the slopes of a cell three times and the trace
 // sources four times per cell; evaluating each once gives the same bits.
-#include "e2d_common.cuh"
-#include "e2d_f64_exact.cuh"
-#include "e2d_internal.h"
+#include "e2d_fp64_blocks.cuh"
 #include "e2d_tma.cuh"
 
 #include <cudaTypedefs.h>
@@ -30,13 +28,6 @@
 
 namespace e2d {
 namespace {
-
-using f64x::gt0;
-using f64x::half;
-using f64x::max_nn;
-using f64x::max_pos;
-using f64x::max_any;
-using f64x::min_any;
 
 constexpr int FILL_BX = 64, FILL_BY = 4;
 
@@ -53,270 +44,6 @@ constexpr size_t flux_smem_bytes() {
 template <int TX, int TY>
 constexpr size_t step_smem_bytes() {
   return flux_smem_bytes<TX, TY>() + 128;
-}
-
-__device__ __forceinline__ int src_lo_hi(int i, int n, int bc_lo, int bc_hi, bool &flip) {
-  return ghost_source(i, n, bc_lo, bc_hi, flip);
-}
-__device__ __forceinline__ bool nonfinite(double x) { return nonfinite64(x); }
-
-// ------------------------------------------------------------ numerics
-// src/HydroBaseFunctor.h:76-102 (computePrimitives) without the sound speed.
-__device__ __forceinline__ void primitives(const KPhys<double> &ph, double rho, double e, double mx,
-                                           double my, double &d, double &p, double &ux, double &uy) {
-  d = max_pos(rho, ph.smallr);
-  ux = mx / d;
-  uy = my / d;
-  const double eken = half(ux * ux + uy * uy);
-  const double ei = e / d - eken;
-  p = max_pos(ph.gm1 * d * ei, d * ph.smallp);
-}
-
-// src/HydroBaseFunctor.h:475-516 for one variable and direction: slope_type
-// 0 gives a zero slope, 1 and 2 the limited slope.
-__device__ __forceinline__ double slope(int st_kind, double q, double qp, double qm) {
-  if (st_kind == 0) return 0.0;
-  return f64x::slope_limited(st_kind == 2, q, qp, qm);
-}
-
-// Sources of trace_unsplit_2d_along_dir (src/HydroBaseFunctor.h:246-249).
-__device__ __forceinline__ void trace_sources(const KPhys<double> &ph, const double q[4],
-                                              const double dqx[4], const double dqy[4], double s0[4]) {
-  const double r = q[E2D_ID], p = q[E2D_IP], u = q[E2D_IU], v = q[E2D_IV];
-  const double drx = dqx[E2D_ID], dpx = dqx[E2D_IP], dux = dqx[E2D_IU], dvx = dqx[E2D_IV];
-  const double dry = dqy[E2D_ID], dpy = dqy[E2D_IP], duy = dqy[E2D_IU], dvy = dqy[E2D_IV];
-  s0[E2D_ID] = -u * drx - v * dry - (dux + dvy) * r;
-  s0[E2D_IP] = -u * dpx - v * dpy - (dux + dvy) * ph.gamma0 * p;
-  s0[E2D_IU] = -u * dux - v * duy - (dpx) / r;
-  s0[E2D_IV] = -u * dvx - v * dvy - (dpy) / r;
-}
-
-// The two face states of one direction (src/HydroBaseFunctor.h:251-289):
-// minus face q - dq/2 + s0*dtd/2, plus face q + dq/2 + s0*dtd/2, density
-// clamped at smallr.
-__device__ __forceinline__ void face_pair(const KPhys<double> &ph, int v, double q, double dq,
-                                          double s0, double dtd, double &fm, double &fp) {
-  const double h = half(dq);
-  const double sx = half(s0 * dtd);
-  fm = q - h + sx;
-  fp = q + h + sx;
-  if (v == E2D_ID) {
-    fm = max_pos(fm, ph.smallr);
-    fp = max_pos(fp, ph.smallr);
-  }
-}
-
-// src/HydroBaseFunctor.h:523-547.
-__device__ __forceinline__ void cmpflx(const KPhys<double> &ph, const double g[4], double f[4]) {
-  f[E2D_ID] = g[E2D_ID] * g[E2D_IU];
-  f[E2D_IU] = f[E2D_ID] * g[E2D_IU] + g[E2D_IP];
-  f[E2D_IV] = f[E2D_ID] * g[E2D_IV];
-  const double ekin = 0.5 * g[E2D_ID] * (g[E2D_IU] * g[E2D_IU] + g[E2D_IV] * g[E2D_IV]);
-  const double etot = g[E2D_IP] * ph.entho + ekin;
-  f[E2D_IP] = g[E2D_IU] * (etot + g[E2D_IP]);
-}
-
-// src/HydroBaseFunctor.h:558-693 (riemann_approx).
-__device__ __noinline__ void riemann_approx(const KPhys<double> &ph, const double *ql,
-                                            const double *qr, double *flux) {
-  const double gamma0 = ph.gamma0, gamma6 = ph.gamma6;
-  const double rl = fmax(ql[E2D_ID], ph.smallr), ul = ql[E2D_IU];
-  const double pl = fmax(ql[E2D_IP], rl * ph.smallp);
-  const double rr = fmax(qr[E2D_ID], ph.smallr), ur = qr[E2D_IU];
-  const double pr = fmax(qr[E2D_IP], rr * ph.smallp);
-  const double cl = gamma0 * pl * rl;
-  const double cr = gamma0 * pr * rr;
-  double wl = sqrt(cl);
-  double wr = sqrt(cr);
-  double pstar = fmax(((wr * pl + wl * pr) + wl * wr * (ul - ur)) / (wl + wr), 0.0);
-  double pold = pstar;
-  double conv = 1.0;
-  for (int iter = 0; (iter < 10) && (conv > 1e-6); ++iter) {
-    const double wwl = sqrt(cl * (1.0 + gamma6 * (pold - pl) / pl));
-    const double wwr = sqrt(cr * (1.0 + gamma6 * (pold - pr) / pr));
-    const double qxl = 2.0 * wwl * wwl * wwl / (wwl * wwl + cl);
-    const double qxr = 2.0 * wwr * wwr * wwr / (wwr * wwr + cr);
-    const double usl = ul - (pold - pl) / wwl;
-    const double usr = ur + (pold - pr) / wwr;
-    const double delp = fmax(qxr * qxl / (qxr + qxl) * (usl - usr), -pold);
-    pold = pold + delp;
-    conv = fabs(delp / (pold + ph.smallpp));
-  }
-  pstar = pold;
-  wl = sqrt(cl * (1.0 + gamma6 * (pstar - pl) / pl));
-  wr = sqrt(cr * (1.0 + gamma6 * (pstar - pr) / pr));
-  const double ustar = 0.5 * (ul + (pl - pstar) / wl + ur - (pr - pstar) / wr);
-  const double sgnm = copysign(1.0, ustar);
-  const bool lft = sgnm > 0.0;
-  const double ro = lft ? rl : rr, uo = lft ? ul : ur, po = lft ? pl : pr, wo = lft ? wl : wr;
-  const double co = fmax(ph.smallc, sqrt(fabs(gamma0 * po / ro)));
-  const double rstar = fmax((ro / (1.0 + ro * (po - pstar) / (wo * wo))), ph.smallr);
-  const double cstar = fmax(ph.smallc, sqrt(fabs(gamma0 * pstar / rstar)));
-  double spout = co - sgnm * uo;
-  double spin = cstar - sgnm * ustar;
-  const double ushock = wo / ro - sgnm * uo;
-  if (pstar >= po) {
-    spin = ushock;
-    spout = ushock;
-  }
-  const double scr = fmax(spout - spin, ph.smallc + fabs(spout + spin));
-  double frac = 0.5 * (1.0 + (spout + spin) / scr);
-  if (frac != frac)
-    frac = 0.0;
-  else
-    frac = frac >= 1.0 ? 1.0 : frac <= 0.0 ? 0.0 : frac;
-  double g[4];
-  g[E2D_ID] = frac * rstar + (1.0 - frac) * ro;
-  g[E2D_IU] = frac * ustar + (1.0 - frac) * uo;
-  g[E2D_IP] = frac * pstar + (1.0 - frac) * po;
-  if (spout < 0.0) {
-    g[E2D_ID] = ro;
-    g[E2D_IU] = uo;
-    g[E2D_IP] = po;
-  }
-  if (spin > 0.0) {
-    g[E2D_ID] = rstar;
-    g[E2D_IU] = ustar;
-    g[E2D_IP] = pstar;
-  }
-  g[E2D_IV] = lft ? ql[E2D_IV] : qr[E2D_IV];
-  cmpflx(ph, g, flux);
-}
-
-// src/HydroBaseFunctor.h:704-809 (riemann_hllc).  The reference builds the
-// star states of both sides and keeps one; here only the star state of the
-// side the contact selects (ustar > 0: left) is built, which yields the same
-// value.  Cut-offs,
-// maxima, the 0.5 factors and the sign tests use the exact integer forms of
-// e2d_f64_exact.cuh.
-__device__ __forceinline__ void riemann_hllc(const KPhys<double> &ph, const double *ql,
-                                             const double *qr, double *flux) {
-  const double rl = max_pos(ql[E2D_ID], ph.smallr);
-  const double pl = max_pos(ql[E2D_IP], rl * ph.smallp);
-  const double ul = ql[E2D_IU];
-  const double hrl = half(rl);
-  double ecinl = hrl * ul * ul;
-  ecinl = ecinl + hrl * ql[E2D_IV] * ql[E2D_IV];
-  const double etotl = pl * ph.entho + ecinl;
-  const double rr = max_pos(qr[E2D_ID], ph.smallr);
-  const double pr = max_pos(qr[E2D_IP], rr * ph.smallp);
-  const double ur = qr[E2D_IU];
-  const double hrr = half(rr);
-  double ecinr = hrr * ur * ur;
-  ecinr = ecinr + hrr * qr[E2D_IV] * qr[E2D_IV];
-  const double etotr = pr * ph.entho + ecinr;
-  const double cfastl = sqrt(max_pos(ph.gamma0 * pl / rl, ph.smallc2));
-  const double cfastr = sqrt(max_pos(ph.gamma0 * pr / rr, ph.smallc2));
-  const double cmax = max_nn(cfastl, cfastr);
-  const double SL = min_any(ul, ur) - cmax;
-  const double SR = max_any(ul, ur) + cmax;
-  const double rcl = rl * (ul - SL);
-  const double rcr = rr * (SR - ur);
-  const double ustar = (rcr * ur + rcl * ul + (pl - pr)) / (rcr + rcl);
-  const double ptotstar = (rcr * pl + rcl * pr + rcl * rcr * (ul - ur)) / (rcr + rcl);
-  const bool lft = gt0(ustar);
-  const double S = lft ? SL : SR;
-  const double rs = lft ? rl : rr, us = lft ? ul : ur, ps = lft ? pl : pr;
-  const double es = lft ? etotl : etotr;
-  const double sdu = S - us;
-  const double sds = S - ustar;
-  const double rstar = rs * sdu / sds;
-  const double etotstar = (sdu * es - ps * us + ptotstar * ustar) / sds;
-  double ro, uo, ptoto, etoto;
-  if (gt0(SL)) {
-    ro = rl, uo = ul, ptoto = pl, etoto = etotl;
-  } else if (lft || gt0(SR)) {
-    ro = rstar, uo = ustar, ptoto = ptotstar, etoto = etotstar;
-  } else {
-    ro = rr, uo = ur, ptoto = pr, etoto = etotr;
-  }
-  flux[E2D_ID] = ro * uo;
-  flux[E2D_IU] = flux[E2D_ID] * uo + ptoto;
-  flux[E2D_IP] = (etoto + ptoto) * uo;
-  flux[E2D_IV] = gt0(flux[E2D_ID]) ? flux[E2D_ID] * ql[E2D_IV] : flux[E2D_ID] * qr[E2D_IV];
-}
-
-// HLL flux (Harten, Lax, van Leer; Toro, "Riemann Solvers and Numerical
-// Methods for Fluid Dynamics", 3rd ed., eq. 10.21).  The reference declares
-// RIEMANN_HLL but has no solver; this uses riemann_hllc's cut-offs and Davis
-// wave speeds; the star flux multiplies by one reciprocal of SR - SL.
-// Operation order matches the oracle's riemann_hll.
-__device__ __forceinline__ void riemann_hll(const KPhys<double> &ph, const double *ql,
-                                            const double *qr, double *flux) {
-  const double rl = max_pos(ql[E2D_ID], ph.smallr);
-  const double pl = max_pos(ql[E2D_IP], rl * ph.smallp);
-  const double ul = ql[E2D_IU], vl = ql[E2D_IV];
-  const double rr = max_pos(qr[E2D_ID], ph.smallr);
-  const double pr = max_pos(qr[E2D_IP], rr * ph.smallp);
-  const double ur = qr[E2D_IU], vr = qr[E2D_IV];
-  const double hrl = half(rl), hrr = half(rr);
-  double ecinl = hrl * ul * ul;
-  ecinl = ecinl + hrl * vl * vl;
-  const double etotl = pl * ph.entho + ecinl;
-  double ecinr = hrr * ur * ur;
-  ecinr = ecinr + hrr * vr * vr;
-  const double etotr = pr * ph.entho + ecinr;
-  const double cfastl = sqrt(max_pos(ph.gamma0 * pl / rl, ph.smallc2));
-  const double cfastr = sqrt(max_pos(ph.gamma0 * pr / rr, ph.smallc2));
-  const double cmax = max_nn(cfastl, cfastr);
-  const double SL = min_any(ul, ur) - cmax;
-  const double SR = max_any(ul, ur) + cmax;
-  const double UL[4] = {rl, etotl, rl * ul, rl * vl};
-  const double UR[4] = {rr, etotr, rr * ur, rr * vr};
-  double FL[4], FR[4];
-  FL[E2D_ID] = UL[E2D_IU];
-  FL[E2D_IP] = (etotl + pl) * ul;
-  FL[E2D_IU] = UL[E2D_IU] * ul + pl;
-  FL[E2D_IV] = UL[E2D_IU] * vl;
-  FR[E2D_ID] = UR[E2D_IU];
-  FR[E2D_IP] = (etotr + pr) * ur;
-  FR[E2D_IU] = UR[E2D_IU] * ur + pr;
-  FR[E2D_IV] = UR[E2D_IU] * vr;
-  if (gt0(SL)) {
-#pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = FL[v];
-  } else if (f64x::le0(SR)) {
-#pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = FR[v];
-  } else {
-    // one division: the four star fluxes share the factor 1 / (SR - SL)
-    const double sls = SL * SR;
-    const double rden = 1.0 / (SR - SL);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) flux[v] = (SR * FL[v] - SL * FR[v] + sls * (UR[v] - UL[v])) * rden;
-  }
-}
-
-template <int RS>
-__device__ __forceinline__ void riemann(const KPhys<double> &ph, const double *ql, const double *qr,
-                                        double *flux) {
-  if (RS == E2D_RIEMANN_HLLC)
-    riemann_hllc(ph, ql, qr, flux);
-  else if (RS == E2D_RIEMANN_HLL)
-    riemann_hll(ph, ql, qr, flux);
-  else
-    riemann_approx(ph, ql, qr, flux);
-}
-
-// ------------------------------------------------------------ kernel 1
-// CFL wave-speed term of a cell from its primitives (src/HydroRunFunctors.h:56-72):
-// (c + |u|) / dx + (c + |v|) / dy, c = sqrt(gamma p / d); a division by a
-// power-of-two dx, dy is the exact product by its reciprocal.
-__device__ __forceinline__ double cfl_term(const KPhys<double> &ph, double dd, double p, double ux, double uy) {
-  const double c = sqrt(ph.gamma0 * p / dd);
-  const double vx = c + fabs(ux);
-  const double vy = c + fabs(uy);
-  const double tx = ph.inv_dx_pow2 != 0.0 ? vx * ph.inv_dx_pow2 : vx / ph.dx;
-  const double ty = ph.inv_dy_pow2 != 0.0 ? vy * ph.inv_dy_pow2 : vy / ph.dy;
-  return tx + ty;
-}
-
-// E2D_FLAG_* bits of a cell's conserved values.
-__device__ __forceinline__ unsigned int state_flags(double rho, double e, double mx, double my) {
-  unsigned int f = 0;
-  if (nonfinite(rho) || nonfinite(e) || nonfinite(mx) || nonfinite(my)) f |= E2D_FLAG_NONFINITE;
-  if (!(rho > 0.0)) f |= E2D_FLAG_DENSITY;
-  return f;
 }
 
 // Ghost fill + primitives + CFL term of array cell (i, j) (see the file
@@ -340,6 +67,12 @@ __device__ __forceinline__ void fill_cell(const KParams64 &kp, double *__restric
   if (fu) mx = -mx;
   if (fv) my = -my;
   const size_t d = (size_t)i + (size_t)g.isize * j;
+  if (mode & FILL_COPY_OUT) {
+    u_out[d] = rho;
+    u_out[d + g.plane] = e;
+    u_out[d + 2 * g.plane] = mx;
+    u_out[d + 3 * g.plane] = my;
+  }
   if (ghost) {
     if (mode & FILL_GHOSTS_IN) {
       u_in[d] = rho;
@@ -417,14 +150,6 @@ __global__ void __launch_bounds__(FILL_BX *FILL_BY)
 // 2.09).  Measured on the 4096^2 blast: 15.12 and 15.38 ms per step; smaller
 // tiles (16 x 16, 32 x 8: 16.1, 16.7 ms) lose more to halo work than they
 // gain in residency.  Results do not depend on the shape.
-// dt of a step from the CFL maximum (src/main.cpp:128-134).
-__device__ __forceinline__ double step_dt(const KPhys<double> &ph, unsigned long long invdt_bits, double t,
-                                          double t_end) {
-  const double inv_dt = __longlong_as_double((long long)invdt_bits);
-  double dt = ph.cfl / inv_dt;
-  if (t + dt > t_end) dt = t_end - t;
-  return dt;
-}
 
 // Shared memory of a tile: primitives with a 2-cell halo, then the face
 // states (the scaled fluxes replace the XMIN / YMIN states in stage 3).
@@ -501,7 +226,7 @@ __device__ __forceinline__ void gather_qtile(const KGeom &g, const double *__res
 // -- src/HydroBaseFunctor.h:214-291 --, then one Riemann solve per face.
 // On return (after a block barrier) sXm holds the x-fluxes scaled by dt/dx
 // and sYm the y-fluxes scaled by dt/dy.
-template <int RS, int TX, int TY, int NT>
+template <int RS, int TX, int TY, int NT, bool FAST = false>
 __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const double dtdx, const double dtdy,
                                             double *smem) {
   using T = TileSmem<TX, TY>;
@@ -528,13 +253,19 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
       dqy[v] = slope(st_kind, qc[v], P[c + QW], P[c - QW]);
     }
     double s0[4];
-    trace_sources(ph, qc, dqx, dqy, s0);
+    if (FAST)
+      trace_sources_fast(ph, qc, dqx, dqy, s0);
+    else
+      trace_sources(ph, qc, dqx, dqy, s0);
     if (yin) {
       const int o = (yy - 1) * XW + xx;
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         double fm, fp;
-        face_pair(ph, v, qc[v], dqx[v], s0[v], dtdx, fm, fp);
+        if (FAST)
+          face_pair_fast(ph, v, qc[v], dqx[v], s0[v], 0.5 * dtdx, fm, fp);
+        else
+          face_pair(ph, v, qc[v], dqx[v], s0[v], dtdx, fm, fp);
         if (xx >= 1) sXm[v * TY * XW + o] = fm;
         if (xx <= TX) sXp[v * TY * XW + o] = fp;
       }
@@ -544,7 +275,10 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         double fm, fp;
-        face_pair(ph, v, qc[v], dqy[v], s0[v], dtdy, fm, fp);
+        if (FAST)
+          face_pair_fast(ph, v, qc[v], dqy[v], s0[v], 0.5 * dtdy, fm, fp);
+        else
+          face_pair(ph, v, qc[v], dqy[v], s0[v], dtdy, fm, fp);
         if (yy >= 1) sYm[v * YH * TX + o] = fm;
         if (yy <= TY) sYp[v * YH * TX + o] = fp;
       }
@@ -566,7 +300,7 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
         ql[v] = sXp[v * TY * XW + ol];
         qr[v] = sXm[v * TY * XW + orr];
       }
-      riemann<RS>(ph, ql, qr, f);
+      riemann_sel<RS, FAST>(ph, ql, qr, f);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sXm[v * TY * XW + orr] = f[v] * dtdx;
     } else {
@@ -580,7 +314,7 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
         ql[vs] = sYp[v * YH * TX + ol];
         qr[vs] = sYm[v * YH * TX + orr];
       }
-      riemann<RS>(ph, ql, qr, f);
+      riemann_sel<RS, FAST>(ph, ql, qr, f);
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
@@ -734,7 +468,7 @@ __host__ __device__ constexpr unsigned int qtile_bytes() {
 //    only interior cells of u_in, which no block writes;
 //  - the last block to finish advances the loop state.
 // Bit-identical to the two-launch step; FP64 work per cell is the same.
-template <int RS, int TX, int TY, int NT, int MINB>
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f64(const KParams64 kp, const __grid_constant__ CUtensorMap tm_q, const int use_tma,
                const double *__restrict__ q_in, double *__restrict__ q_out, double *__restrict__ u_in,
@@ -792,7 +526,7 @@ __global__ void __launch_bounds__(NT, MINB)
   double term = 0.0;
   unsigned int flags = 0;
   if (ok) {
-    tile_fluxes<RS, TX, TY, NT>(ph, s_dt[1], s_dt[2], smem);
+    tile_fluxes<RS, TX, TY, NT, FAST>(ph, s_dt[1], s_dt[2], smem);
     const TileSmem<TX, TY> sm(smem);
     for (int k = tid; k < TX * TY; k += NT) {
       const int y = k / TX, x = k - y * TX;
@@ -805,13 +539,16 @@ __global__ void __launch_bounds__(NT, MINB)
           un[v] = update_var<TX, TY>(sm, v, x, y, u_in[s + v * g.plane]);
           u_out[s + v * g.plane] = un[v];
         }
-        double dd, p, ux, uy;
-        primitives(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy);
+        double dd, p, ux, uy, rd = 0.0;
+        if (FAST)
+          primitives_fast(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy, rd);
+        else
+          primitives(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy);
         q_out[s] = dd;
         q_out[s + g.plane] = p;
         q_out[s + 2 * g.plane] = ux;
         q_out[s + 3 * g.plane] = uy;
-        term = fmax(term, cfl_term(ph, dd, p, ux, uy));
+        term = fmax(term, FAST ? cfl_term_fast(ph, rd, p, ux, uy) : cfl_term(ph, dd, p, ux, uy));
         flags |= state_flags(un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV]);
       }
     }
@@ -1108,9 +845,9 @@ static cudaError_t set_flux_smem() {
                               (int)flux_smem_bytes<TX, TY>());
 }
 
-template <int RS, int TX, int TY, int NT, int MINB>
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false>
 static cudaError_t set_step_smem() {
-  return cudaFuncSetAttribute(k_step_f64<RS, TX, TY, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_step_f64<RS, TX, TY, NT, MINB, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)step_smem_bytes<TX, TY>());
 }
 
@@ -1122,6 +859,7 @@ static cudaError_t configure_rs() {
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 16, 256, 2>();
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 31, 512, 1>();
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 15, 256, 2>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 32, 512, 1, true>();
   return e;
 }
 
@@ -1186,13 +924,13 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
 // (2047 Riemann solves: four full rounds of 512 threads); 3 -> 32 x 15 (two
 // blocks per SM, 1007 solves: four rounds of 256).  Results do not depend on
 // the shape.
-template <int RS, int TX, int TY, int NT, int MINB>
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false>
 static cudaError_t launch_step_shape(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                      double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
                                      cudaStream_t s) {
   dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
-  k_step_f64<RS, TX, TY, NT, MINB><<<grid, NT, step_smem_bytes<TX, TY>(), s>>>(kp, tm_q, use_tma, q_in, q_out, u_in,
-                                                                                u_out, clk, dt_trace);
+  k_step_f64<RS, TX, TY, NT, MINB, FAST><<<grid, NT, step_smem_bytes<TX, TY>(), s>>>(kp, tm_q, use_tma, q_in, q_out,
+                                                                                      u_in, u_out, clk, dt_trace);
   return cudaGetLastError();
 }
 
@@ -1200,6 +938,8 @@ template <int RS>
 static cudaError_t launch_step_t(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                  double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
                                  cudaStream_t s) {
+  if (kp.fast)  // the fast forms: 32 x 32 tiles only
+    return launch_step_shape<RS, 32, 32, 512, 1, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
   switch (kp.tile) {
     case 1: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
     case 2: return launch_step_shape<RS, 32, 31, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
@@ -1235,7 +975,7 @@ bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp) {
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
   if (!encode || (kp.g.isize & 1) || (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
-  const int ty = kp.tile == 1 ? 16 : kp.tile == 2 ? 31 : kp.tile == 3 ? 15 : 32;
+  const int ty = kp.fast ? 32 : kp.tile == 1 ? 16 : kp.tile == 2 ? 31 : kp.tile == 3 ? 15 : 32;
   const cuuint64_t dims[3] = {(cuuint64_t)kp.g.isize, (cuuint64_t)kp.g.jsize, 4};
   const cuuint64_t strides[2] = {(cuuint64_t)kp.g.isize * sizeof(double), (cuuint64_t)kp.g.plane * sizeof(double)};
   const cuuint32_t box[3] = {32 + 4, (cuuint32_t)ty + 4, 4};

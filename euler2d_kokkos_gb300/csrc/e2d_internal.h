@@ -52,12 +52,14 @@ struct KPhys {
   // 1/dx, 1/dy when dx, dy are powers of two (then x / dx == x * (1/dx) bit
   // for bit: both round the same exact value), else 0
   R inv_dx_pow2, inv_dy_pow2;
+  R inv_dx, inv_dy;  // 1/dx, 1/dy rounded (E2D_PRECISION_FP64_FAST only)
 };
 
 struct KParams64 {
   KGeom g;
   KPhys<double> ph;
   int tile;       // flux / fused step kernel tile shape (see launch_step_f64)
+  int fast;       // E2D_PRECISION_FP64_FAST: the fused step's fast forms (not bit-identical)
   int wait_test;  // nonzero: tile (1, 1) of the fused step never stages its primitives,
                   // so its bounded wait runs out (E2D_TEST_WAIT_TIMEOUT=1; tests the timeout path)
 };
@@ -112,6 +114,7 @@ enum : int {
   FILL_GHOSTS_OUT = 4,       // store the ghost fill into the output state (deep_copy)
   FILL_DT = 8,               // fold the CFL term of interior cells into clock->invdt_bits (or acc[slot])
   FILL_DEVICE_CLOCK = 16,    // do nothing once clock->t >= clock->t_end
+  FILL_COPY_OUT = 32,        // copy the whole ghost-filled input state into the output (deep_copy)
 };
 
 // FP64 kernels (e2d_fp64.cu, bit-identical to the reference).
@@ -124,6 +127,14 @@ cudaError_t launch_fill_f64(const KParams64 &kp, double *u_in, double *u_out, do
 cudaError_t launch_step_f64(const KParams64 &kp, int riemann, const CUtensorMap &tm_q, int use_tma,
                             const double *q_in, double *q_out, double *u_in, double *u_out, DevClock *clk,
                             double *dt_trace, cudaStream_t s);
+// The reference's implementations 1 and 2 of the step (e2d_impl12.cu), after
+// a fill with FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_COPY_OUT (and FILL_DT |
+// FILL_DEVICE_CLOCK in the device loop, use_clock = 1); implementation 1 needs
+// impl12_scratch_doubles(kp, 1) doubles of scratch.
+size_t impl12_scratch_doubles(const KParams64 &kp, int impl);
+cudaError_t launch_impl12_f64(const KParams64 &kp, int impl, int riemann, const double *q, double *u_out,
+                              double *scratch, DevClock *clk, int use_clock, double host_dt, double *dt_trace,
+                              cudaStream_t s);
 // TMA map of a primitives array for the fused step's tile shape; false if
 // isize is odd or the driver cannot encode it (tiles are gathered then).
 bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp);

@@ -55,9 +55,13 @@ enum {
   E2D_PROBLEM_SHOCKED_BUBBLE = 4
 };
 enum { E2D_LAYOUT_LEFT = 0, E2D_LAYOUT_RIGHT = 1 };
-/* Arithmetic of the step: FP64 (bit-identical to the reference) or FP32
- * with a compensated hi/lo conservative update. */
-enum { E2D_PRECISION_FP64 = 0, E2D_PRECISION_FP32C = 1 };
+/* Arithmetic of the step: FP64 (bit-identical to the reference), FP32 with
+ * a compensated hi/lo conservative update, or FP64 "fast" (opt-in: FMAs and
+ * shared Newton-refined reciprocals in the step; within 1e-12 of the
+ * reference on dt and 1e-10 relative L1 in the tests, not bit-identical;
+ * e2d_step_n only -- e2d_godunov_unsplit, batches and the allocation-free
+ * entry point refuse it with E2D_EINVAL). */
+enum { E2D_PRECISION_FP64 = 0, E2D_PRECISION_FP32C = 1, E2D_PRECISION_FP64_FAST = 2 };
 
 /* Flat mirror of HydroParams + HydroSettings (src/HydroParams.h:107-265).
  * Fill it with e2d_params_from_ini (the reference's ini semantics, reals

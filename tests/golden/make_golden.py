@@ -16,6 +16,7 @@ Outputs (small, committed):
     sedov.npz     the Sedov post-processing (src/main.cpp:175-179) of a 64x64
                   point blast after 60 steps: the .npy files the reference's
                   ComputeRadialProfileFunctor writes, for three ring counts
+    impl.npz      the reference's implementations 1 and 2 on four run cases
     vtk.npz       HydroRun::saveVTK output: the .vti bytes of a 32x24 state
                   and the SHA-256 of the .vti of the C1 state
 
@@ -202,6 +203,36 @@ def gen_c1(R: ReferenceLib, tmp: str) -> dict:
             "l1_interior": [float(np.abs(interior[v]).sum()).hex() for v in range(4)]}
 
 
+IMPL_CASES = ("blast_reflect", "periodic_smooth", "mixed_bc_smooth", "implode_diag")
+
+
+def gen_impl(R: ReferenceLib, tmp: str) -> dict:
+    """The reference's implementations 1 and 2 ([OTHER] implementationVersion)
+    on four of the run cases: dt of every step and the final state.  (The
+    reference's implementation 2 adds fluxes with atomics; under OpenMP the
+    order of those additions varies between runs at the rounding level.)"""
+    out = {}
+    cases = C.run_cases()
+    for name in IMPL_CASES:
+        case = cases[name]
+        for impl in (1, 2):
+            text = case["ini"] + f"\n[OTHER]\nimplementationVersion={impl}\n"
+            path = C.write_ini(text, tmp, f"impl{impl}_{name}.ini")
+            u0 = case["inject"]() if case["inject"] else None
+            u, dts, t, ns = R.run(path, u0, case["nsteps"])
+            key = f"{name}__impl{impl}"
+            out[f"{key}__ini"] = np.array(text)
+            out[f"{key}__t"] = np.array(t)
+            out[f"{key}__nsteps"] = np.array(ns)
+            if impl == 1:  # SHA-256 of the bits (they are implementation 0's: runs.npz)
+                out[f"{key}__sha256"] = np.array(hashlib.sha256(np.ascontiguousarray(u).tobytes()
+                                                                + np.ascontiguousarray(dts).tobytes()).hexdigest())
+            else:
+                out[f"{key}__dt"] = dts
+                out[f"{key}__u"] = u
+    return out
+
+
 VTK_SMALL_INI = C.ini_text(32, 24, problem="implode", gamma0=1.666, xmin=-1.0, xmax=1.0)
 
 
@@ -250,7 +281,7 @@ def main():
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", choices=["params", "kat", "runs", "c1", "sedov", "vtk"])
+    ap.add_argument("--only", choices=["params", "kat", "runs", "c1", "sedov", "vtk", "impl"])
     only = ap.parse_args().only
     R = ReferenceLib()
     tmp = tempfile.mkdtemp(prefix="e2d_golden_")
@@ -264,6 +295,8 @@ def main():
     if only in (None, "c1"):
         with open(os.path.join(HERE, "c1.json"), "w") as f:
             json.dump(gen_c1(R, tmp), f, indent=1)
+    if only in (None, "impl"):
+        np.savez_compressed(os.path.join(HERE, "impl.npz"), **gen_impl(R, tmp))
     if only in (None, "vtk"):
         np.savez_compressed(os.path.join(HERE, "vtk.npz"), **gen_vtk(R, tmp))
     if only in (None, "sedov"):

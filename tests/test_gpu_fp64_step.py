@@ -80,7 +80,7 @@ def test_fused_step_stops_at_t_end_and_resumes(gpu_lib, monkeypatch):
     with e2d.HydroRun(p, init_problem=False) as h:
         h.set_state(0, u0)
         h.set_state(1, u0)
-        t, ns, tr1 = h.step_n(9, 10.0, 0.0, 0)
+        t, ns, tr1 = h.step_n(5, 0.01, 0.0, 0)
         t, ns, tr2 = h.step_n(64, 0.01, t, ns)  # t_end reached inside the call
         u = h.current(ns)
     op = po.make_params(nx, ny, gamma0=1.4, cfl=0.8, slope_type=2.0, bc=bc, riemann="hllc")
