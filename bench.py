@@ -66,7 +66,8 @@ def parse():
                          "step at every tile shape, fused and as two launches; fp64peak: the FP64 "
                          "operation rates of this GPU")
     ap.add_argument("--instances", type=int, default=512)
-    ap.add_argument("--sample", type=int, default=24, help="solves timed one at a time (batch mode)")
+    ap.add_argument("--sample", type=int, default=0,
+                    help="solves timed one at a time in --mode batch (0: all of them)")
     ap.add_argument("--rates", default="", help="arrival rates (solves/s) for serve mode, comma-separated")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--c3-nx", type=int, default=8192, help="grid side of --mode c3")
@@ -422,6 +423,15 @@ def fp64_ops_per_cell(riemann, tile=0, fast=False):
 _FP64_RATES = None
 
 
+def fp64_pipe_counts(kernel):
+    """FP64-pipe instructions per cell of a kernel from the committed ncu
+    capture (profiles/fp64_pipe.json), or None."""
+    path = os.path.join(ROOT, "profiles", "fp64_pipe.json")
+    if not os.path.exists(path):
+        return None
+    return json.load(open(path)).get(kernel)
+
+
 def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0, fast=False):
     """FP64-pipe roofline of the fused step, live: the probe's measured rates
     (e2d_fp64_rates, this run), the source-counted operations per cell in FMA
@@ -441,8 +451,19 @@ def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0, fast=False):
     achieved = per_cell * cells / (kernel_ms * 1e-3) / 1e9
     out.update({"ops_per_cell": ops, "fma_equivalent_per_cell": per_cell,
                 "cost_in_fma": {k: cost[k] for k in ("addmul", "div", "sqrt", "max")},
-                "achieved_gops": achieved, "frac": achieved / r["fma"],
-                "ops_source": "counted from k_step_f64's source (bench.py F64_OPS)"})
+                "achieved_gops": achieved, "frac_algorithmic": achieved / r["fma"],
+                "ops_source": "counted from k_step_f64's source (bench.py F64_OPS), divisions and square "
+                              "roots weighted by their measured cost"})
+    # the instructions the FP64 pipe actually executes per cell (one ncu
+    # capture of this kernel; the division and square-root sequences and the
+    # compiler add to the source count) at the live cell rate: the pipe's
+    # busy fraction, as ncu's sm__pipe_fp64_cycles_active measures it
+    ic = fp64_pipe_counts(f"k_step_f64<{riemann}>" + (" fast" if fast else ""))
+    if ic:
+        inst = ic["fp64_pipe_inst_per_cell"] * cells / (kernel_ms * 1e-3) / 1e9
+        out.update({"fp64_pipe_inst_per_cell": ic["fp64_pipe_inst_per_cell"], "achieved_inst_gops": inst,
+                    "frac": inst / r["fma"], "ncu_busy_pct_same_kernel": ic.get("fp64_pipe_busy_pct"),
+                    "inst_source": ic.get("source")})
     return out
 
 
@@ -514,6 +535,12 @@ SERVE_WORKLOAD = ("Poisson arrivals of blasts, four-quadrant problems and shocke
                   "density ratio 0.1..10), grids 64^2..2048^2, t_end U[0.05,0.25], 150 GB pool, HLLC, CFL 0.8")
 
 
+def size_quartiles(solves):
+    """Grid cells (nx * ny) of a set of solves: min, quartiles, max."""
+    c = np.array([s.cells for s in solves], dtype=np.float64)
+    return [int(x) for x in np.percentile(c, [0, 25, 50, 75, 100])]
+
+
 def batch_summary(instances, sample, fp64=False):
     """Mixed 64^2-1024^2 blasts and four-quadrant problems (seed 0), each to
     its own t_end: one batched run of all of them against the same kind of
@@ -525,8 +552,11 @@ def batch_summary(instances, sample, fp64=False):
 
     prec = e2d.PRECISION_FP64 if fp64 else e2d.PRECISION_FP32C
     solves = workloads.mixed_batch(instances, seed=0, precision=prec)
+    # the one-at-a-time sample: every k-th solve in order of grid size, so
+    # that it spans the mix's size distribution (sample >= instances: all)
+    by_size = sorted(range(len(solves)), key=lambda k: (solves[k].cells, k))
     stride = max(1, len(solves) // sample)
-    sample_idx = list(range(0, len(solves), stride))[:sample]
+    sample_idx = sorted(by_size[stride // 2::stride][:sample]) if sample < len(solves) else list(range(len(solves)))
     # accuracy: the smallest sampled solves against the FP64 path
     small = [] if fp64 else sorted(sample_idx, key=lambda k: solves[k].cells)[:3]
     bstats, states = serving.run_batched(solves, pool_bytes=64 << 30, keep=set(small))
@@ -546,7 +576,11 @@ def batch_summary(instances, sample, fp64=False):
                               "cell_updates": seq.cell_updates,
                               "rerun_fp64_after_nonfinite": [sample_idx[k] for k in seq.escalated],
                               "failed": [sample_idx[k] for k in seq.failed],
-                              "sample": f"{len(sample_idx)} of the {len(solves)} solves, every {stride}th"},
+                              "sample": (f"all {len(solves)} solves" if len(sample_idx) == len(solves) else
+                                         f"{len(sample_idx)} of the {len(solves)} solves: every {stride}th in "
+                                         f"order of grid size"),
+                              "cells_quartiles_sample": size_quartiles([solves[k] for k in sample_idx]),
+                              "cells_quartiles_mix": size_quartiles(solves)},
             "batched_over_one_at_a_time": bstats.gcell_per_s / seq.gcell_per_s if seq.gcell_per_s else None,
             **out_l1}
 
@@ -581,9 +615,13 @@ def mode_line(value, mode, config_, extra):
 
 
 def batch_mode(args):
+    """The C4 batches with every solve also run one at a time (--sample
+    defaults to all of them here)."""
+    sample = args.instances if args.sample <= 0 else args.sample
     with ClockSampler(0) as clocks:
-        b = batch_summary(args.instances, args.sample)
-        b64 = batch_summary(max(8, args.instances // 8), max(2, args.sample // 3), fp64=True)
+        b = batch_summary(args.instances, sample)
+        b64 = batch_summary(max(8, args.instances // 8), max(8, args.instances // 8) if args.sample <= 0
+                            else max(2, args.sample // 3), fp64=True)
     line = mode_line(b["value"], "batch", {"workload": b["workload"], "instances": b["instances"],
                                            "cells_total": b["cells_total"], "tuning": b["tuning"]},
                      {**{k: b[k] for k in ("batched", "one_at_a_time", "batched_over_one_at_a_time",
@@ -665,17 +703,23 @@ def f64tiles_mode(args):
     rows = []
     with ClockSampler(0) as clocks:
         for rs in ("hllc", "hll"):
-            for label, env in [("fused 32x32", {"E2D_F64_TILE": "0"}), ("fused 32x16", {"E2D_F64_TILE": "1"}),
-                               ("fused 32x31", {"E2D_F64_TILE": "2"}), ("fused 32x15", {"E2D_F64_TILE": "3"}),
-                               ("two launches 32x32", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"})]:
-                m = measure(e2d, torch, args, "fp64", "blast", nx, args.steps, args.warmup, 0, bar, None,
+            for label, prec, env in [
+                    ("fused 32x32", "fp64", {"E2D_F64_TILE": "0"}),
+                    ("fused 32x32, 2 solves per thread", "fp64", {"E2D_F64_TILE": "0", "E2D_F64_ILP": "2"}),
+                    ("fused 32x16", "fp64", {"E2D_F64_TILE": "1"}),
+                    ("fused 32x31", "fp64", {"E2D_F64_TILE": "2"}), ("fused 32x15", "fp64", {"E2D_F64_TILE": "3"}),
+                    ("two launches 32x32", "fp64", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"}),
+                    ("fast, fused 32x32", "fp64_fast", {"E2D_F64_TILE": "0"}),
+                    ("fast, fused 32x32, 2 solves per thread", "fp64_fast", {"E2D_F64_TILE": "0", "E2D_F64_ILP": "2"})]:
+                m = measure(e2d, torch, args, prec, "blast", nx, args.steps, args.warmup, 0, bar, None,
                             with_e2e=False, with_clocks=False, riemann=rs, env=env)
                 kt = {k: round(v[0] / v[1], 4) for k, v in m["kernels"].items()}
                 row = {"riemann": rs, "form": label, "ms_per_step": m["ms"] / args.steps,
                        "gcell_per_s": cells * args.steps / (m["ms"] / 1e3) / 1e9, "kernel_ms_avg": kt}
-                if label.startswith("fused"):
+                if "fused" in label:
                     k = next(k for k in kt if k.startswith("k_step_f64"))
-                    row["fp64_pipe"] = fp64_pipe_info(e2d, rs, kt[k], cells, int(env["E2D_F64_TILE"]))
+                    row["fp64_pipe"] = fp64_pipe_info(e2d, rs, kt[k], cells, int(env["E2D_F64_TILE"]),
+                                                      fast=prec == "fp64_fast")
                 rows.append(row)
     line = {"metric": METRIC, "mode": "f64tiles", "config": config("blast", nx, "hllc/hll", "fp64"),
             "steps": args.steps, "rows": rows, "clocks": clocks.summary()}
@@ -814,8 +858,8 @@ def main():
             "accuracy": l1_steps(e2d, args.problem, nx, args.steps, precs=("fp64", "fp64_fast")),
             "tolerance": "dt within 1e-12 relative, relative L1 <= 1e-10 (tests/test_gpu_fp64_fast.py)"}
         # batched mixed solves against one at a time, and one loaded serving point
-        line["batch"] = batch_summary(512, 24)
-        line["batch_fp64"] = batch_summary(64, 8, fp64=True)
+        line["batch"] = batch_summary(512, 64)
+        line["batch_fp64"] = batch_summary(64, 16, fp64=True)
         line["serve"] = {"workload": SERVE_WORKLOAD, "sweep": serve_summary([32.0], 10.0, 320)}
 
     if rank == 0 and not args.no_cpu_baseline:

@@ -105,6 +105,8 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->ph.inv_dx = 1.0 / p.dx;
   kp->ph.inv_dy = 1.0 / p.dy;
   kp->fast = p.precision == E2D_PRECISION_FP64_FAST ? 1 : 0;
+  kp->ilp = 1;
+  if (const char *v = std::getenv("E2D_F64_ILP")) kp->ilp = std::atoi(v) == 2 ? 2 : 1;
   kp->tile = 0;
   if (const char *v = std::getenv("E2D_F64_TILE")) kp->tile = std::atoi(v);
   const char *wt = std::getenv("E2D_TEST_WAIT_TIMEOUT");

@@ -264,5 +264,6 @@ def test_profiling_mode_same_bits(gpu_lib, runs, tmp_path):
         u, dts, t, ns = run_device_loop(h, runs[f"{name}__u0"], 60, 10.0)
         kt = h.kernel_times()
     assert np.array_equal(u, runs[f"{name}__u"])
-    assert any(k.startswith("k_flux_update_f64") for k in kt)
-    assert all(c == 60 for _, c in kt.values())
+    assert any(k.startswith("k_step_f64") for k in kt)
+    # one prologue per device-loop call, one fused step per step
+    assert all(c == (1 if k.endswith("(prologue)") else 60) for k, (_, c) in kt.items())
