@@ -31,7 +31,9 @@ double *g_scratch_ptr[kMaxDevices] = {};  // device address of the scratch, per 
 std::mutex g_setup_mutex;
 
 // Once per device, with that device current: the device address of the
-// scratch symbol and the kernels' shared-memory limit.
+// scratch symbol and the kernels' shared-memory limit.  Both are kept for the
+// life of the process; after a cudaDeviceReset the cached address would be
+// stale, so calls after a reset are not supported (include/e2d.h says so).
 int setup_device(int dev, double **out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_ptr[dev]) {

@@ -218,7 +218,10 @@ int e2d_godunov_unsplit(e2d_sim *sim, int nStep, double dt);
  * shared-memory limit) with that device current; make that first call
  * before any stream capture.  All calls on a device share the one array, so
  * calls that overlap on the GPU (different streams, or host threads without
- * ordering) race with each other; serialise them.  FP64 precision only. */
+ * ordering) race with each other; serialise them.  The address and the limit
+ * are kept for the life of the process: calls after cudaDeviceReset (or any
+ * other teardown of the device's primary context) are not supported.  FP64
+ * precision only. */
 #define E2D_NOALLOC_MAX_CELLS (1 << 18)
 int e2d_godunov_unsplit_noalloc(const e2d_params *p, double *u_in, double *u_out, double dt,
                                 void *stream);
@@ -227,10 +230,13 @@ int e2d_godunov_unsplit_noalloc(const e2d_params *p, double *u_in, double *u_out
  * each step takes dt = cfl/max wave speed of the current state, clamps it to
  * t_end - t, runs godunov_unsplit and advances (t, nStep); steps with
  * t >= t_end do nothing.  *t and *nStep are read and updated.  dt_trace
- * (optional, n entries) receives the dt of each step taken.  Launches are
- * replayed from cached CUDA graphs.  Blocks until done.  E2D_ENUMERIC: a
- * step saw a non-finite state or dt; E2D_ETIMEOUT: a row-staging wait of the
- * TMA variant gave up (the state of this call is incomplete; the handle stays
+ * (optional, n entries) receives the dt of each step taken.  FP64: one
+ * prologue kernel (primitives and CFL maximum of the input state), then one
+ * fused kernel per step whose epilogue folds the next step's CFL maximum;
+ * launches are replayed from cached CUDA graphs.  Blocks until done.
+ * E2D_ENUMERIC: a step saw a non-finite state or dt; E2D_ETIMEOUT: a bounded
+ * wait for a TMA copy (FP64 tile staging, FP32C row staging of the TMA
+ * variant) gave up (the state of this call is incomplete; the handle stays
  * usable). */
 int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double *dt_trace);
 
