@@ -579,6 +579,7 @@ def batch_summary(instances, sample, fp64=False):
                               "sample": (f"all {len(solves)} solves" if len(sample_idx) == len(solves) else
                                          f"{len(sample_idx)} of the {len(solves)} solves: every {stride}th in "
                                          f"order of grid size"),
+                              "sample_indices": sample_idx,
                               "cells_quartiles_sample": size_quartiles([solves[k] for k in sample_idx]),
                               "cells_quartiles_mix": size_quartiles(solves)},
             "batched_over_one_at_a_time": bstats.gcell_per_s / seq.gcell_per_s if seq.gcell_per_s else None,

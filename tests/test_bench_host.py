@@ -39,6 +39,8 @@ def test_batch_summary_reports_reruns_and_failures(monkeypatch):
         assert out["value"] == 2.0 and out["batched_over_one_at_a_time"] == 20.0
         assert out["batched"]["rerun_fp64_after_nonfinite"] == [3] and out["batched"]["failed"] == [5]
         # one-at-a-time indices are mapped back to the batch's solve numbers
-        assert out["one_at_a_time"]["rerun_fp64_after_nonfinite"] == [4]
+        idx = out["one_at_a_time"]["sample_indices"]
+        assert len(idx) == 4 and idx == sorted(idx)
+        assert out["one_at_a_time"]["rerun_fp64_after_nonfinite"] == [idx[1]]
         assert out["precision"] == ("fp64" if fp64 else "fp32c")
         assert out["instances"] == 16
