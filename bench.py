@@ -399,10 +399,18 @@ F64_OPS_FAST = {
     "hll": {"addmul": 42, "fma": 26, "sqrt": 2},
     "epilogue": {"addmul": 28, "fma": 7, "sqrt": 1, "max": 4},
 }
-F64_TILES = {0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}
+F64_TILES = {-1: (32, 16), 0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}  # E2D_F64_TILE -> shape
 
 
-def fp64_ops_per_cell(riemann, tile=0, fast=False):
+def tile_shape(tile, fast=False):
+    """(TX, TY) of the fused FP64 step for an E2D_F64_TILE value (the fast
+    forms exist for 32 x 16 and 32 x 32)."""
+    if fast:
+        return (32, 32) if tile == 0 else (32, 16)
+    return F64_TILES.get(tile, (32, 16))
+
+
+def fp64_ops_per_cell(riemann, tile=-1, fast=False):
     """FP64 operations per cell-update of the fused step by kind, for a tile
     shape: per tile, (TX+2)(TY+2)-4 slope/trace evaluations, 2 TX TY + 2 TX
     + 2 TY face-pair directions, (TX+1) TY + TX (TY+1) solves and TX TY
@@ -410,7 +418,7 @@ def fp64_ops_per_cell(riemann, tile=0, fast=False):
     ops = F64_OPS_FAST if fast else F64_OPS
     if riemann not in ops:
         return None
-    tx, ty = (32, 32) if fast else F64_TILES.get(tile, (32, 32))
+    tx, ty = tile_shape(tile, fast)
     n = {"slopes_trace": (tx + 2) * (ty + 2) - 4, "faces_dir": 2 * tx * ty + 2 * tx + 2 * ty,
          riemann: (tx + 1) * ty + tx * (ty + 1), "epilogue": tx * ty}
     tot = {"addmul": 0.0, "fma": 0.0, "div": 0.0, "sqrt": 0.0, "max": 0.0}
@@ -432,7 +440,7 @@ def fp64_pipe_counts(kernel):
     return json.load(open(path)).get(kernel)
 
 
-def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0, fast=False):
+def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=-1, fast=False):
     """FP64-pipe roofline of the fused step, live: the probe's measured rates
     (e2d_fp64_rates, this run), the source-counted operations per cell in FMA
     equivalents, and the fraction of the FMA peak the kernel sustained."""
@@ -458,7 +466,8 @@ def fp64_pipe_info(e2d, riemann, kernel_ms, cells, tile=0, fast=False):
     # capture of this kernel; the division and square-root sequences and the
     # compiler add to the source count) at the live cell rate: the pipe's
     # busy fraction, as ncu's sm__pipe_fp64_cycles_active measures it
-    ic = fp64_pipe_counts(f"k_step_f64<{riemann}>" + (" fast" if fast else ""))
+    tx, ty = tile_shape(tile, fast)
+    ic = fp64_pipe_counts(f"k_step_f64<{riemann}>" + (" fast" if fast else "") + f" {tx}x{ty}")
     if ic:
         inst = ic["fp64_pipe_inst_per_cell"] * cells / (kernel_ms * 1e-3) / 1e9
         out.update({"fp64_pipe_inst_per_cell": ic["fp64_pipe_inst_per_cell"], "achieved_inst_gops": inst,
@@ -705,13 +714,12 @@ def f64tiles_mode(args):
     with ClockSampler(0) as clocks:
         for rs in ("hllc", "hll"):
             for label, prec, env in [
+                    ("fused 32x16 (default)", "fp64", {"E2D_F64_TILE": "1"}),
                     ("fused 32x32", "fp64", {"E2D_F64_TILE": "0"}),
-                    ("fused 32x32, 2 solves per thread", "fp64", {"E2D_F64_TILE": "0", "E2D_F64_ILP": "2"}),
-                    ("fused 32x16", "fp64", {"E2D_F64_TILE": "1"}),
                     ("fused 32x31", "fp64", {"E2D_F64_TILE": "2"}), ("fused 32x15", "fp64", {"E2D_F64_TILE": "3"}),
                     ("two launches 32x32", "fp64", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"}),
-                    ("fast, fused 32x32", "fp64_fast", {"E2D_F64_TILE": "0"}),
-                    ("fast, fused 32x32, 2 solves per thread", "fp64_fast", {"E2D_F64_TILE": "0", "E2D_F64_ILP": "2"})]:
+                    ("fast, fused 32x16 (default)", "fp64_fast", {"E2D_F64_TILE": "1"}),
+                    ("fast, fused 32x32", "fp64_fast", {"E2D_F64_TILE": "0"})]:
                 m = measure(e2d, torch, args, prec, "blast", nx, args.steps, args.warmup, 0, bar, None,
                             with_e2e=False, with_clocks=False, riemann=rs, env=env)
                 kt = {k: round(v[0] / v[1], 4) for k, v in m["kernels"].items()}
@@ -789,7 +797,7 @@ def main():
     if roof and f64:
         roof["note"] = "the FP64 step is bound by GB300's FP64 pipe, not HBM: see fp64_pipe"
         roof["fp64_pipe"] = fp64_pipe_info(e2d, args.riemann, roof["kernel_ms_avg"], cells,
-                                           int(os.environ.get("E2D_F64_TILE", "0")),
+                                           int(os.environ.get("E2D_F64_TILE", "-1")),
                                            fast=args.precision == "fp64_fast")
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms"] / args.steps,

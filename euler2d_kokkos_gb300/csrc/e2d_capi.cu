@@ -105,9 +105,7 @@ void e2d::make_kparams(const e2d_params &p, KParams64 *kp) {
   kp->ph.inv_dx = 1.0 / p.dx;
   kp->ph.inv_dy = 1.0 / p.dy;
   kp->fast = p.precision == E2D_PRECISION_FP64_FAST ? 1 : 0;
-  kp->ilp = 1;
-  if (const char *v = std::getenv("E2D_F64_ILP")) kp->ilp = std::atoi(v) == 2 ? 2 : 1;
-  kp->tile = 0;
+  kp->tile = -1;
   if (const char *v = std::getenv("E2D_F64_TILE")) kp->tile = std::atoi(v);
   const char *wt = std::getenv("E2D_TEST_WAIT_TIMEOUT");
   kp->wait_test = (wt && std::atoi(wt) != 0) ? 1 : 0;

@@ -226,7 +226,7 @@ __device__ __forceinline__ void gather_qtile(const KGeom &g, const double *__res
 // -- src/HydroBaseFunctor.h:214-291 --, then one Riemann solve per face.
 // On return (after a block barrier) sXm holds the x-fluxes scaled by dt/dx
 // and sYm the y-fluxes scaled by dt/dy.
-template <int RS, int TX, int TY, int NT, bool FAST = false, int ILP = 1>
+template <int RS, int TX, int TY, int NT, bool FAST = false>
 __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const double dtdx, const double dtdy,
                                             double *smem) {
   using T = TileSmem<TX, TY>;
@@ -287,60 +287,38 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
   __syncthreads();
 
   // stage 3: one Riemann solve per face; the scaled flux replaces the
-  // right-hand state, which no other face reads.  With ILP = 2 a thread
-  // runs two independent solves side by side (faces k and k + NT), so that
-  // twice as many FP64 results are in flight per warp; a thread without a
-  // second face repeats its first solve and stores it once.  Every solve of
-  // an iteration loads its states before any of its stores.
+  // right-hand state, which no other face reads
   constexpr int NXF = (TX + 1) * TY;
   constexpr int NYF = TX * (TY + 1);
-  constexpr int NF = NXF + NYF;
-  for (int k0 = tid; k0 < NF; k0 += ILP * NT) {
-    double ql[ILP][4], qr[ILP][4], f[ILP][4];
-    int dst[ILP];
-    bool isy[ILP], live[ILP];
+  for (int k = tid; k < NXF + NYF; k += NT) {
+    double ql[4], qr[4], f[4];
+    if (k < NXF) {
+      const int y = k / (TX + 1), fx = k - y * (TX + 1);
+      const int ol = y * XW + fx, orr = ol + 1;
 #pragma unroll
-    for (int u = 0; u < ILP; ++u) {
-      live[u] = k0 + u * NT < NF;
-      const int k = live[u] ? k0 + u * NT : k0;
-      isy[u] = k >= NXF;
-      if (!isy[u]) {
-        const int y = k / (TX + 1), fx = k - y * (TX + 1);
-        const int ol = y * XW + fx;
-        dst[u] = ol + 1;
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          ql[u][v] = sXp[v * TY * XW + ol];
-          qr[u][v] = sXm[v * TY * XW + ol + 1];
-        }
-      } else {
-        const int kk = k - NXF;
-        const int fy = kk / TX, x = kk - fy * TX;
-        const int ol = fy * TX + x;
-        dst[u] = ol + TX;
-        // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
-          ql[u][vs] = sYp[v * YH * TX + ol];
-          qr[u][vs] = sYm[v * YH * TX + ol + TX];
-        }
+      for (int v = 0; v < 4; ++v) {
+        ql[v] = sXp[v * TY * XW + ol];
+        qr[v] = sXm[v * TY * XW + orr];
       }
-    }
+      riemann_sel<RS, FAST>(ph, ql, qr, f);
 #pragma unroll
-    for (int u = 0; u < ILP; ++u) riemann_sel<RS, FAST>(ph, ql[u], qr[u], f[u]);
+      for (int v = 0; v < 4; ++v) sXm[v * TY * XW + orr] = f[v] * dtdx;
+    } else {
+      const int kk = k - NXF;
+      const int fy = kk / TX, x = kk - fy * TX;
+      const int ol = fy * TX + x, orr = ol + TX;
+      // normal velocity first: swap IU/IV (src/HydroRunFunctors.h:628-632)
 #pragma unroll
-    for (int u = 0; u < ILP; ++u) {
-      if (!live[u]) continue;
-      if (!isy[u]) {
+      for (int v = 0; v < 4; ++v) {
+        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
+        ql[vs] = sYp[v * YH * TX + ol];
+        qr[vs] = sYm[v * YH * TX + orr];
+      }
+      riemann_sel<RS, FAST>(ph, ql, qr, f);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) sXm[v * TY * XW + dst[u]] = f[u][v] * dtdx;
-      } else {
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
-          sYm[v * YH * TX + dst[u]] = f[u][vs] * dtdy;
-        }
+      for (int v = 0; v < 4; ++v) {
+        const int vs = (v == E2D_IU) ? E2D_IV : (v == E2D_IV) ? E2D_IU : v;
+        sYm[v * YH * TX + orr] = f[vs] * dtdy;
       }
     }
   }
@@ -490,7 +468,7 @@ __host__ __device__ constexpr unsigned int qtile_bytes() {
 //    only interior cells of u_in, which no block writes;
 //  - the last block to finish advances the loop state.
 // Bit-identical to the two-launch step; FP64 work per cell is the same.
-template <int RS, int TX, int TY, int NT, int MINB, bool FAST, int ILP>
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST>
 __global__ void __launch_bounds__(NT, MINB)
     k_step_f64(const KParams64 kp, const __grid_constant__ CUtensorMap tm_q, const int use_tma,
                const double *__restrict__ q_in, double *__restrict__ q_out, double *__restrict__ u_in,
@@ -548,7 +526,7 @@ __global__ void __launch_bounds__(NT, MINB)
   double term = 0.0;
   unsigned int flags = 0;
   if (ok) {
-    tile_fluxes<RS, TX, TY, NT, FAST, ILP>(ph, s_dt[1], s_dt[2], smem);
+    tile_fluxes<RS, TX, TY, NT, FAST>(ph, s_dt[1], s_dt[2], smem);
     const TileSmem<TX, TY> sm(smem);
     for (int k = tid; k < TX * TY; k += NT) {
       const int y = k / TX, x = k - y * TX;
@@ -867,9 +845,9 @@ static cudaError_t set_flux_smem() {
                               (int)flux_smem_bytes<TX, TY>());
 }
 
-template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false, int ILP = 1>
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false>
 static cudaError_t set_step_smem() {
-  return cudaFuncSetAttribute(k_step_f64<RS, TX, TY, NT, MINB, FAST, ILP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_step_f64<RS, TX, TY, NT, MINB, FAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)step_smem_bytes<TX, TY>());
 }
 
@@ -882,8 +860,7 @@ static cudaError_t configure_rs() {
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 31, 512, 1>();
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 15, 256, 2>();
   if (e == cudaSuccess) e = set_step_smem<RS, 32, 32, 512, 1, true>();
-  if (e == cudaSuccess) e = set_step_smem<RS, 32, 32, 512, 1, false, 2>();
-  if (e == cudaSuccess) e = set_step_smem<RS, 32, 32, 512, 1, true, 2>();
+  if (e == cudaSuccess) e = set_step_smem<RS, 32, 16, 256, 2, true>();
   return e;
 }
 
@@ -943,17 +920,18 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
   }
 }
 
-// Fused-step tile shapes (kp.tile): 0 -> 32 x 32 cells, 512 threads, one
-// block per SM; 1 -> 32 x 16, 256 threads, two blocks per SM; 2 -> 32 x 31
-// (2047 Riemann solves: four full rounds of 512 threads); 3 -> 32 x 15 (two
-// blocks per SM, 1007 solves: four rounds of 256).  Results do not depend on
-// the shape.
-template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false, int ILP = 1>
+// Fused-step tile shapes (kp.tile): 32 x 16 cells, 256 threads, two blocks
+// per SM (the default: 17.61 ms per 4096^2 HLLC step); 0 -> 32 x 32, 512
+// threads, one block per SM (17.85 ms); 2 -> 32 x 31 (2047 Riemann solves:
+// four full rounds of 512 threads; 17.80 ms); 3 -> 32 x 15 (two blocks per
+// SM, 1007 solves: four rounds of 256; 17.77 ms).  The fast forms exist for
+// 32 x 16 and 32 x 32.  Results do not depend on the shape.
+template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false>
 static cudaError_t launch_step_shape(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                      double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
                                      cudaStream_t s) {
   dim3 grid((kp.g.nx + TX - 1) / TX, (kp.g.ny + TY - 1) / TY);
-  k_step_f64<RS, TX, TY, NT, MINB, FAST, ILP><<<grid, NT, step_smem_bytes<TX, TY>(), s>>>(kp, tm_q, use_tma, q_in, q_out,
+  k_step_f64<RS, TX, TY, NT, MINB, FAST><<<grid, NT, step_smem_bytes<TX, TY>(), s>>>(kp, tm_q, use_tma, q_in, q_out,
                                                                                       u_in, u_out, clk, dt_trace);
   return cudaGetLastError();
 }
@@ -962,20 +940,17 @@ template <int RS>
 static cudaError_t launch_step_t(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                  double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
                                  cudaStream_t s) {
-  if (kp.fast) {  // the fast forms: 32 x 32 tiles only
-    if (kp.ilp == 2)
-      return launch_step_shape<RS, 32, 32, 512, 1, true, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk,
-                                                            dt_trace, s);
-    return launch_step_shape<RS, 32, 32, 512, 1, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+  if (kp.fast) {  // the fast forms: 32 x 16 (default) and 32 x 32 tiles
+    if (kp.tile == 0)
+      return launch_step_shape<RS, 32, 32, 512, 1, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace,
+                                                         s);
+    return launch_step_shape<RS, 32, 16, 256, 2, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
   }
-  if (kp.ilp == 2 && kp.tile == 0)
-    return launch_step_shape<RS, 32, 32, 512, 1, false, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk,
-                                                           dt_trace, s);
   switch (kp.tile) {
-    case 1: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    case 0: return launch_step_shape<RS, 32, 32, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
     case 2: return launch_step_shape<RS, 32, 31, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
     case 3: return launch_step_shape<RS, 32, 15, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
-    default: return launch_step_shape<RS, 32, 32, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    default: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
   }
 }
 
@@ -1006,7 +981,7 @@ bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp) {
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
   if (!encode || (kp.g.isize & 1) || (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
-  const int ty = kp.fast ? 32 : kp.tile == 1 ? 16 : kp.tile == 2 ? 31 : kp.tile == 3 ? 15 : 32;
+  const int ty = kp.tile == 0 ? 32 : kp.tile == 2 && !kp.fast ? 31 : kp.tile == 3 && !kp.fast ? 15 : 16;
   const cuuint64_t dims[3] = {(cuuint64_t)kp.g.isize, (cuuint64_t)kp.g.jsize, 4};
   const cuuint64_t strides[2] = {(cuuint64_t)kp.g.isize * sizeof(double), (cuuint64_t)kp.g.plane * sizeof(double)};
   const cuuint32_t box[3] = {32 + 4, (cuuint32_t)ty + 4, 4};

@@ -109,3 +109,17 @@ def test_fused_step_wait_runs_out_with_etimeout(gpu_lib, monkeypatch):
         h.set_state(1, u0)
         t, ns, _ = h.step_n(2, 10.0, 0.0, 0)
         assert ns == 2 and np.isfinite(h.current(ns)).all()
+
+
+def test_fast_forms_do_not_depend_on_the_tile_shape(gpu_lib, monkeypatch):
+    """The fast forms (not bit-identical to the reference) still give one
+    result whatever the tile: 32 x 16 (default) and 32 x 32 agree bit for bit."""
+    nx, ny, bc = GRIDS[0]
+    p = params(nx, ny, bc)
+    p.precision = e2d.PRECISION_FP64_FAST
+    p.init()
+    u0 = C.smooth_state(nx, ny, G14, seed=5)
+    a = run_loop(p, u0, 15, 15, {"E2D_F64_TILE": "0"}, monkeypatch)
+    b = run_loop(p, u0, 15, 15, {"E2D_F64_TILE": "1"}, monkeypatch)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
