@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--rates", default="", help="arrival rates (solves/s) for serve mode, comma-separated")
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--c3-nx", type=int, default=8192, help="grid side of --mode c3")
+    ap.add_argument("--repeat", type=int, default=0, help="--mode f64tiles: interleaved repeats of the HLLC forms")
     a = ap.parse_args()
     if a.problem is None:
         a.problem = "four_quadrant" if a.precision == "fp32c" else "blast"
@@ -702,7 +703,10 @@ def c3_mode(args):
 
 def f64tiles_mode(args):
     """The FP64 blast (--nx, HLLC and HLL) at every fused-step tile shape and
-    as two launches per step, CUDA events on the library's stream."""
+    as two launches per step, CUDA events on the library's stream.  With
+    --repeat R the HLLC forms are measured R times in turn instead and the
+    line gives each form's median (timings of the forms interleave, so that
+    drifts of the GPU affect them alike)."""
     import torch
 
     import euler2d_kokkos_gb300 as e2d
@@ -711,6 +715,22 @@ def f64tiles_mode(args):
     cells = nx * nx
     bar = torch.cuda.synchronize
     rows = []
+    if args.repeat > 0:
+        forms = [("fused 32x16", {"E2D_F64_TILE": "1"}), ("fused 32x32", {"E2D_F64_TILE": "0"}),
+                 ("two launches 32x32", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"})]
+        got = {f: [] for f, _ in forms}
+        with ClockSampler(0) as clocks:
+            for _ in range(args.repeat):
+                for label, env in forms:
+                    m = measure(e2d, torch, args, "fp64", "blast", nx, args.steps, args.warmup, 0, bar, None,
+                                with_e2e=False, with_clocks=False, riemann="hllc", env=env)
+                    got[label].append(m["ms"] / args.steps)
+        rows = [{"form": f, "ms_per_step_median": float(np.median(v)), "ms_per_step": v,
+                 "gcell_per_s_median": cells / (float(np.median(v)) / 1e3) / 1e9} for f, v in got.items()]
+        print(json.dumps({"metric": METRIC, "mode": "f64tiles", "repeat": args.repeat, "steps": args.steps,
+                          "config": config("blast", nx, "hllc", "fp64"), "rows": rows,
+                          "clocks": clocks.summary()}), flush=True)
+        return
     with ClockSampler(0) as clocks:
         for rs in ("hllc", "hll"):
             for label, prec, env in [
