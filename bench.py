@@ -400,15 +400,15 @@ F64_OPS_FAST = {
     "hll": {"addmul": 42, "fma": 26, "sqrt": 2},
     "epilogue": {"addmul": 28, "fma": 7, "sqrt": 1, "max": 4},
 }
-F64_TILES = {-1: (32, 16), 0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}  # E2D_F64_TILE -> shape
+F64_TILES = {-1: (32, 32), 0: (32, 32), 1: (32, 16), 2: (32, 31), 3: (32, 15)}  # E2D_F64_TILE -> shape
 
 
 def tile_shape(tile, fast=False):
     """(TX, TY) of the fused FP64 step for an E2D_F64_TILE value (the fast
     forms exist for 32 x 16 and 32 x 32)."""
     if fast:
-        return (32, 32) if tile == 0 else (32, 16)
-    return F64_TILES.get(tile, (32, 16))
+        return (32, 16) if tile == 1 else (32, 32)
+    return F64_TILES.get(tile, (32, 32))
 
 
 def fp64_ops_per_cell(riemann, tile=-1, fast=False):
@@ -734,12 +734,12 @@ def f64tiles_mode(args):
     with ClockSampler(0) as clocks:
         for rs in ("hllc", "hll"):
             for label, prec, env in [
-                    ("fused 32x16 (default)", "fp64", {"E2D_F64_TILE": "1"}),
-                    ("fused 32x32", "fp64", {"E2D_F64_TILE": "0"}),
+                    ("fused 32x32 (default)", "fp64", {"E2D_F64_TILE": "0"}),
+                    ("fused 32x16", "fp64", {"E2D_F64_TILE": "1"}),
                     ("fused 32x31", "fp64", {"E2D_F64_TILE": "2"}), ("fused 32x15", "fp64", {"E2D_F64_TILE": "3"}),
                     ("two launches 32x32", "fp64", {"E2D_F64_SPLIT": "1", "E2D_F64_TILE": "0"}),
-                    ("fast, fused 32x16 (default)", "fp64_fast", {"E2D_F64_TILE": "1"}),
-                    ("fast, fused 32x32", "fp64_fast", {"E2D_F64_TILE": "0"})]:
+                    ("fast, fused 32x32 (default)", "fp64_fast", {"E2D_F64_TILE": "0"}),
+                    ("fast, fused 32x16", "fp64_fast", {"E2D_F64_TILE": "1"})]:
                 m = measure(e2d, torch, args, prec, "blast", nx, args.steps, args.warmup, 0, bar, None,
                             with_e2e=False, with_clocks=False, riemann=rs, env=env)
                 kt = {k: round(v[0] / v[1], 4) for k, v in m["kernels"].items()}

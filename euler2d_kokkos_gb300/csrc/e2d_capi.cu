@@ -28,6 +28,12 @@ struct e2d_sim {
   int q_tma = 0;                      // FP64: both maps encoded (isize even)
   int f64_split = 0;                  // FP64 device loop as two launches per step (E2D_F64_SPLIT=1)
   int impl = 0;                       // FP64: implementationVersion (1, 2: the debug orchestrations)
+  // FP64 fused step: the parity whose primitives (Q[par], interior) and CFL
+  // maximum (q_acc) on the device are those of U[par] as the last device-loop
+  // call left them, so the next call needs no prologue; -1 once anything may
+  // have changed a state
+  int q_ready = -1;
+  unsigned long long q_acc = 0ull;
   double *impl_scratch = nullptr;     // FP64, implementation 1: stored slopes and fluxes
   float *W[2] = {nullptr, nullptr};   // FP32C: compensated U and U2 (8 float planes)
   CUtensorMap TM[2];                  // FP32C: TMA maps of W[0], W[1] (row staging)
@@ -383,6 +389,7 @@ int e2d_get_stream(e2d_sim *s, void **stream) {
 
 int e2d_device_state(e2d_sim *s, int which, double **dptr) {
   if (!s || !dptr || (which != 0 && which != 1)) return E2D_EINVAL;
+  s->q_ready = -1;  // the caller may write through the pointer
   int rc = fp64_view(s, which, dptr);
   if (rc != E2D_OK) return rc;
   if (s->fp32) E2D_CK(s, cudaStreamSynchronize(s->stream), "device_state sync");
@@ -391,6 +398,7 @@ int e2d_device_state(e2d_sim *s, int which, double **dptr) {
 
 int e2d_init_problem(e2d_sim *s) {
   if (!s) return E2D_EINVAL;
+  s->q_ready = -1;
   if (s->fp32) {
     E2D_CK(s, launch_init_f64(s->kp, s->p, s->stage, s->stream), "init problem");
     E2D_CK(s, launch_f32c_from_f64(s->kp32, s->stage, s->W[0], s->stream), "init convert");
@@ -406,6 +414,7 @@ int e2d_init_problem(e2d_sim *s) {
 int e2d_set_state(e2d_sim *s, int which, const double *host, int layout) {
   if (!s || !host || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad set_state args");
   if (layout != E2D_LAYOUT_LEFT && layout != E2D_LAYOUT_RIGHT) return set_err(s, E2D_EINVAL, "bad layout");
+  s->q_ready = -1;
   const size_t n = 4 * cells(s);
   std::vector<double> tmp;
   const double *src = host;
@@ -488,6 +497,7 @@ int e2d_save_vtk(e2d_sim *s, int which, const char *filename) {
 
 int e2d_make_boundaries(e2d_sim *s, int which) {
   if (!s || (which != 0 && which != 1)) return set_err(s, E2D_EINVAL, "bad make_boundaries args");
+  s->q_ready = -1;
   // FP32C states keep no ghost cells: every reader maps them on the fly
   if (s->fp32) return E2D_OK;
   E2D_CK(s, launch_fill_f64(s->kp, s->U[which], nullptr, nullptr, s->clk, FILL_GHOSTS_IN, s->stream), "make_boundaries");
@@ -515,6 +525,7 @@ int e2d_compute_dt(e2d_sim *s, int useU, double *dt) {
 int e2d_godunov_unsplit(e2d_sim *s, int nStep, double dt) {
   if (!s) return E2D_EINVAL;
   if (s->kp.fast) return set_err(s, E2D_EINVAL, "fp64_fast runs through the device time loop (e2d_step_n) only");
+  s->q_ready = -1;
   const int par = (nStep % 2 == 0) ? 0 : 1;  // src/HydroRun.h:263-270
   if (s->fp32) {
     E2D_CK(s, launch_f32c_step(s->kp32, s->p.riemannSolverType, s->W[par], s->W[par ^ 1], s->TM[par], s->clk, 0, dt,
@@ -548,9 +559,16 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   c.trace_base = *nStep;
   c.trace_cap = n;
   c.trace = s->dt_trace;
+  const int par0 = (*nStep % 2 == 0) ? 0 : 1;
+  // the fused FP64 step reads the primitives and CFL maximum of its input:
+  // from the previous call when nothing has changed the state since, else
+  // from a prologue fill
+  const bool fused = !s->fp32 && !s->f64_split && s->impl == 0;
+  const bool prologue = fused && s->q_ready != par0;
+  if (fused && !prologue) c.acc[par0] = s->q_acc;
+  s->q_ready = -1;
   *s->clk_host = c;
   E2D_CK(s, cudaMemcpyAsync(s->clk, s->clk_host, sizeof(DevClock), cudaMemcpyHostToDevice, s->stream), "clock upload");
-  const int par0 = (*nStep % 2 == 0) ? 0 : 1;
   // FP32C and the fused FP64 step: the first step's CFL maximum (and the
   // primitives of the input state); later steps fold it in their epilogue
   if (s->fp32) E2D_CK(s, launch_f32c_dt(s->kp32, s->W[par0], s->clk, *nStep & 1, s->stream), "initial dt");
@@ -558,7 +576,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
     size_t ev = 0;
     std::vector<std::pair<std::string, std::pair<cudaEvent_t, cudaEvent_t>>> marks;
     const std::string rs = riemann_name(s->p.riemannSolverType);
-    if (!s->fp32 && !s->f64_split) {
+    if (prologue) {
       cudaEvent_t a = pool_event(s, ev++), b = pool_event(s, ev++);
       if (!a || !b) return set_err(s, E2D_ECUDA, "event create");
       E2D_CK(s, cudaEventRecord(a, s->stream), "event");
@@ -605,7 +623,7 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
       record_kernel(s, m.first, ms);
     }
   } else {
-    E2D_CK(s, enqueue_prologue(s, par0, *nStep), "prologue");
+    if (prologue) E2D_CK(s, enqueue_prologue(s, par0, *nStep), "prologue");
     int done = 0;
     while (n - done >= kGraphSteps) {
       cudaGraphExec_t g;
@@ -628,6 +646,10 @@ int e2d_step_n(e2d_sim *s, int n, double t_end, double *t, int *nStep, double *d
   if (s->clk_host->status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT))
     return set_err(s, E2D_ENUMERIC, (s->clk_host->status & E2D_FLAG_NONFINITE) ? "non-finite state value"
                                                                               : "non-positive or non-finite dt");
+  if (fused) {  // the last step (or the prologue) left U[nStep & 1]'s primitives and CFL maximum
+    s->q_ready = *nStep & 1;
+    s->q_acc = s->clk_host->acc[*nStep & 1];
+  }
   return E2D_OK;
 }
 

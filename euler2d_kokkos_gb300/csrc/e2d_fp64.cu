@@ -920,12 +920,13 @@ cudaError_t launch_flux_update_f64(const KParams64 &kp, int riemann, const doubl
   }
 }
 
-// Fused-step tile shapes (kp.tile): 32 x 16 cells, 256 threads, two blocks
-// per SM (the default: 17.61 ms per 4096^2 HLLC step); 0 -> 32 x 32, 512
-// threads, one block per SM (17.85 ms); 2 -> 32 x 31 (2047 Riemann solves:
-// four full rounds of 512 threads; 17.80 ms); 3 -> 32 x 15 (two blocks per
-// SM, 1007 solves: four rounds of 256; 17.77 ms).  The fast forms exist for
-// 32 x 16 and 32 x 32.  Results do not depend on the shape.
+// Fused-step tile shapes (kp.tile): 32 x 32 cells, 512 threads, one block
+// per SM (the default); 1 -> 32 x 16, 256 threads, two blocks per SM (0.6 %
+// slower per 4096^2 HLLC step: 5 % more instructions per cell for the halo,
+// the FP64 pipe 86 % instead of 82 % busy); 2 -> 32 x 31 (2047 Riemann
+// solves: four full rounds of 512 threads); 3 -> 32 x 15 (two blocks per SM,
+// 1007 solves: four rounds of 256).  The fast forms exist for 32 x 32 and
+// 32 x 16.  Results do not depend on the shape.
 template <int RS, int TX, int TY, int NT, int MINB, bool FAST = false>
 static cudaError_t launch_step_shape(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                      double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
@@ -940,17 +941,17 @@ template <int RS>
 static cudaError_t launch_step_t(const KParams64 &kp, const CUtensorMap &tm_q, int use_tma, const double *q_in,
                                  double *q_out, double *u_in, double *u_out, DevClock *clk, double *dt_trace,
                                  cudaStream_t s) {
-  if (kp.fast) {  // the fast forms: 32 x 16 (default) and 32 x 32 tiles
-    if (kp.tile == 0)
-      return launch_step_shape<RS, 32, 32, 512, 1, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace,
+  if (kp.fast) {  // the fast forms: 32 x 32 (default) and 32 x 16 tiles
+    if (kp.tile == 1)
+      return launch_step_shape<RS, 32, 16, 256, 2, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace,
                                                          s);
-    return launch_step_shape<RS, 32, 16, 256, 2, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    return launch_step_shape<RS, 32, 32, 512, 1, true>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
   }
   switch (kp.tile) {
-    case 0: return launch_step_shape<RS, 32, 32, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    case 1: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
     case 2: return launch_step_shape<RS, 32, 31, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
     case 3: return launch_step_shape<RS, 32, 15, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
-    default: return launch_step_shape<RS, 32, 16, 256, 2>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
+    default: return launch_step_shape<RS, 32, 32, 512, 1>(kp, tm_q, use_tma, q_in, q_out, u_in, u_out, clk, dt_trace, s);
   }
 }
 
@@ -981,7 +982,7 @@ bool encode_q_map(CUtensorMap *map, const double *q, const KParams64 &kp) {
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
   if (!encode || (kp.g.isize & 1) || (reinterpret_cast<uintptr_t>(q) & 15u)) return false;
-  const int ty = kp.tile == 0 ? 32 : kp.tile == 2 && !kp.fast ? 31 : kp.tile == 3 && !kp.fast ? 15 : 16;
+  const int ty = kp.tile == 1 ? 16 : kp.tile == 2 && !kp.fast ? 31 : kp.tile == 3 && !kp.fast ? 15 : 32;
   const cuuint64_t dims[3] = {(cuuint64_t)kp.g.isize, (cuuint64_t)kp.g.jsize, 4};
   const cuuint64_t strides[2] = {(cuuint64_t)kp.g.isize * sizeof(double), (cuuint64_t)kp.g.plane * sizeof(double)};
   const cuuint32_t box[3] = {32 + 4, (cuuint32_t)ty + 4, 4};

@@ -58,8 +58,8 @@ struct KPhys {
 struct KParams64 {
   KGeom g;
   KPhys<double> ph;
-  int tile;       // tile shape: -1 the kernels' defaults (fused step 32 x 16, two-launch flux
-                  // 32 x 32), else see launch_step_f64 and launch_flux_update_f64
+  int tile;       // tile shape: -1 the default (32 x 32), else see launch_step_f64 and
+                  // launch_flux_update_f64
   int fast;       // E2D_PRECISION_FP64_FAST: the fused step's fast forms (not bit-identical)
   int wait_test;  // nonzero: tile (1, 1) of the fused step never stages its primitives,
                   // so its bounded wait runs out (E2D_TEST_WAIT_TIMEOUT=1; tests the timeout path)

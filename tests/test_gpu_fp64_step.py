@@ -123,3 +123,42 @@ def test_fast_forms_do_not_depend_on_the_tile_shape(gpu_lib, monkeypatch):
     b = run_loop(p, u0, 15, 15, {"E2D_F64_TILE": "1"}, monkeypatch)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def test_device_loop_cache_follows_state_changes(gpu_lib):
+    """A device-loop call reuses the primitives and CFL maximum the previous
+    call left on the device only while nothing has changed the state: after
+    set_state, godunov_unsplit or make_boundaries between calls, the result
+    is that of a fresh handle run from the changed state."""
+    nx, ny, bc = GRIDS[0]
+    p = params(nx, ny, bc)
+    ua = C.smooth_state(nx, ny, G14, seed=21)
+    ub = C.smooth_state(nx, ny, G14, seed=22)
+
+    def fresh(u0, steps):
+        with e2d.HydroRun(p, init_problem=False) as f:
+            f.set_state(0, u0)
+            f.set_state(1, u0)
+            t, ns, tr = f.step_n(steps, 10.0, 0.0, 0)
+            return f.current(ns), tr
+
+    with e2d.HydroRun(p, init_problem=False) as h:
+        h.set_state(0, ua)
+        h.set_state(1, ua)
+        h.step_n(4, 10.0, 0.0, 0)          # leaves U's primitives cached
+        h.set_state(0, ub)                 # ... which set_state must drop
+        h.set_state(1, ub)
+        t, ns, tr = h.step_n(6, 10.0, 0.0, 0)
+        u, d = fresh(ub, 6)
+        assert np.array_equal(h.current(ns), u) and np.array_equal(tr, d)
+        # a host-driven step between two device-loop calls
+        dt = h.compute_dt(ns % 2)
+        h.godunov_unsplit(ns, dt)
+        t2, ns2, tr2 = h.step_n(3, 10.0, t + dt, ns + 1)
+        with e2d.HydroRun(p, init_problem=False) as f:
+            f.set_state(0, ub)
+            f.set_state(1, ub)
+            tf, nf, _ = f.step_n(6, 10.0, 0.0, 0)
+            f.godunov_unsplit(nf, f.compute_dt(nf % 2))
+            tf, nf, trf = f.step_n(3, 10.0, tf + dt, nf + 1)
+            assert np.array_equal(h.current(ns2), f.current(nf)) and np.array_equal(tr2, trf)
