@@ -330,15 +330,19 @@ def _measure(e2d, torch, args, precision, problem, nx, steps, warmup, local, bar
         barrier()
         t0 = time.perf_counter()
         h.set_state(0, host_in)
+        t1 = time.perf_counter()
         _, ns2, _ = h.step_n(steps, t_end, 0.0, 0)
+        t2 = time.perf_counter()
         h.get_state(ns2 % 2, host_out)
-        e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+        t3 = time.perf_counter()
+        e2e_s = max_over_ranks(dist, t3 - t0)
         world = dist.get_world_size() if dist else 1
         out["e2e"] = {"value": nx * nx * ns2 * world / e2e_s / 1e9, "unit": METRIC,
                       "h2d_bytes_per_step": host_in.nbytes / max(ns2, 1),
                       "d2h_bytes_per_step": (host_out.nbytes + 8 * ns2) / max(ns2, 1),
                       "path": "e2d_set_state + e2d_step_n + e2d_get_state from pinned host buffers, "
-                              f"{ns2} steps per call"}
+                              f"{ns2} steps per call",
+                      "seconds": {"set_state": t1 - t0, "step_n": t2 - t1, "get_state": t3 - t2}}
     h.close()
     return out
 
