@@ -567,28 +567,36 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     s1 = ghost_source(min(max(c0 + 1, 0), g.isize - 1), g.nx, g.bc_xmin, g.bc_xmax, f1);
   }
   constexpr int R = PFD + 3;  // ring slots; row r sits in slot (r - rb + 2) mod R
+  static_assert(TMA != 2 || R == 6, "row pairs need a ring of three pairs");
   const bool yghost = (rb - 2 < 2) || (re + 1 > g.ny + 1);
-  auto slot_of = [&](int sl) { return ring + sl * SLOT; };
+  // Staged variants: interior strips (`bulk`) fill the ring by TMA copies
+  // and wait on the slots' barriers; boundary strips copy each lane's
+  // boundary-mapped columns by cp.async and wait on commit groups.  With
+  // TMA == 2 (`pairs`) an interior strip away from the ghost rows copies two
+  // rows per TMA request (box 64 x 2 x 8 into a pair of slots laid out plane
+  // by plane, [8][2][64]) and waits once per pair.
+  const bool bulk = (TMA != 0) && (PFD > 0) && direct && !(TMA == 2 && yghost);
+  const bool pairs = (TMA == 2) && bulk;
+  const int ps = pairs ? 128 : 64;  // floats between the planes of a slot
+  auto slot_of = [&](int sl) {
+    return pairs ? ring + (sl >> 1) * (2 * SLOT) + (sl & 1) * 64 : ring + sl * SLOT;
+  };
   auto wrap = [](int x) { return x >= R ? x - R : x; };
   int sm1 = 0;  // slot of row m-1 (the row being updated)
   // hi of a staged row, ghost flips applied
   auto staged_hi = [&](int r, int sl, float2 out[4]) {
     const float *p = slot_of(sl) + 2 * lane;
 #pragma unroll
-    for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(p + v * 64);
+    for (int v = 0; v < 4; ++v) out[v] = *reinterpret_cast<const float2 *>(p + v * ps);
     if (f0) out[E2D_IU].x = -out[E2D_IU].x;
     if (f1) out[E2D_IU].y = -out[E2D_IU].y;
     bool fv;
     source_row(g, r, yghost, fv);
     if (fv) out[E2D_IV] = neg2(out[E2D_IV]);
   };
-  // Staged variants: interior strips (`bulk`) fill the ring by TMA copies
-  // and wait on the slots' barriers; boundary strips copy each lane's
-  // boundary-mapped columns by cp.async and wait on commit groups.
-  const bool bulk = (TMA != 0) && (PFD > 0) && direct;
-  unsigned int pending = 0u;  // slots with a TMA copy not yet waited for
+  unsigned int pending = 0u;  // slots (pairs: pair slots) with a TMA copy not yet waited for
   auto stage = [&](int r, int sl) {
-    if (bulk) {
+    if (bulk && TMA == 1) {
       // wait_test: the first row of strip (1, 0) is never copied
       if (kp.wait_test && sx == 1 && sy == 0 && r == rb - 2) return;
       stage_row_tma(g, map, r, cb - 2, lane, yghost, slot_of(sl), bars + sl);
@@ -601,6 +609,20 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     const bool done = mbar_wait(bars + sl, (phase >> sl) & 1u);
     if (done) phase ^= 1u << sl, pending &= ~(1u << sl);
     return done;
+  };
+  // pairs: rows rb-2+2k and rb-1+2k into pair slot k mod 3 (its barrier k mod
+  // 3); the caller has passed a __syncwarp after every lane's last read of
+  // that pair.  A pair whose first row is past re+1 is not needed.
+  auto stage_pair = [&](int k) {
+    const int r = rb - 2 + 2 * k;
+    if (r > re + 1) return;
+    const int pp = k % 3;
+    fence_proxy_async_smem();
+    if (lane == 0) {
+      mbar_arrive_expect(bars + pp, 2 * kRowBytes);
+      tma_load_3d(ring + pp * (2 * SLOT), map, cb - 2, r, 0, bars + pp);
+    }
+    pending |= 1u << pp;
   };
   // a wait that ran out: flag it, let the copies in flight land (bounded
   // too) before the ring is reused or the block exits, leave the strip;
@@ -616,16 +638,22 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     // the cp.async path), after every lane is done with the ring's previous
     // strip
     __syncwarp();
-    for (int r = rb - 2; r < rb + PFD; ++r) {
-      stage(r, r - rb + 2);
-      if (!bulk) cp_async_commit();
-    }
-    if (bulk) {
-      if (!(wait_slot(0) && wait_slot(1))) {
-        return give_up();
-      }
+    if (pairs) {
+      stage_pair(0);
+      stage_pair(1);
+      if (!wait_slot(0)) return give_up();
     } else {
-      cp_async_wait<(PFD > 0 ? PFD : 0)>();
+      for (int r = rb - 2; r < rb + PFD; ++r) {
+        stage(r, r - rb + 2);
+        if (!bulk) cp_async_commit();
+      }
+      if (bulk) {
+        if (!(wait_slot(0) && wait_slot(1))) {
+          return give_up();
+        }
+      } else {
+        cp_async_wait<(PFD > 0 ? PFD : 0)>();
+      }
     }
     __syncwarp();  // lanes read columns other lanes copied
     float2 u[4];
@@ -650,17 +678,26 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
       // barrier makes every lane's copies visible to the warp and orders
       // every lane's reads of row m-2 (previous iteration) before the copy
       // of row m+1+PFD into that slot
-      if (bulk) {
-        if (!wait_slot(wrap(sm1 + 2))) {
-          return give_up();
-        }
+      if (pairs) {
+        // row m+1 opens pair k = j/2 (j its index in the strip): wait for
+        // it, then refill the pair of rows m-3 and m-2, now dead, with pair k+1
+        const int j = m + 1 - (rb - 2);
+        if (!(j & 1) && !wait_slot((j >> 1) % 3)) return give_up();
+        __syncwarp();
+        if (!(j & 1)) stage_pair((j >> 1) + 1);
       } else {
-        cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
+        if (bulk) {
+          if (!wait_slot(wrap(sm1 + 2))) {
+            return give_up();
+          }
+        } else {
+          cp_async_wait<(PFD > 0 ? PFD - 1 : 0)>();
+        }
+        __syncwarp();
+        const int rn = m + 1 + PFD;
+        if (rn <= re + 1) stage(rn, wrap(sm1 + R - 1));
+        if (!bulk) cp_async_commit();
       }
-      __syncwarp();
-      const int rn = m + 1 + PFD;
-      if (rn <= re + 1) stage(rn, wrap(sm1 + R - 1));
-      if (!bulk) cp_async_commit();
       float2 u[4];
       staged_hi(m + 1, wrap(sm1 + 2), u);
       prims2(k, u[0], u[1], u[2], u[3], qc);
@@ -759,8 +796,8 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
           const float *sl = slot_of(sm1) + 2 * lane;
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
-            uhi[v] = *reinterpret_cast<const float2 *>(sl + v * 64);
-            ulo[v] = *reinterpret_cast<const float2 *>(sl + (4 + v) * 64);
+            uhi[v] = *reinterpret_cast<const float2 *>(sl + v * ps);
+            ulo[v] = *reinterpret_cast<const float2 *>(sl + (4 + v) * ps);
           }
         }
         float2 nh[4];
@@ -1026,6 +1063,18 @@ static void with_variant(int v, F &&f) {
 }
 static_assert(kF32cVariants == 7, "with_variant covers variants 0..6");
 
+// The single-grid step's variants: those of with_variant, plus variant 7
+// (MINB 3, rows staged three ahead, interior strips by one TMA copy per two
+// rows).  Batches keep variants 0..6: their instances' maps have one-row boxes.
+template <class F>
+static void with_step_variant(int v, F &&f) {
+  if (v == 7) {
+    f(std::integral_constant<int, 3>{}, std::integral_constant<int, 3>{}, std::integral_constant<int, 2>{});
+    return;
+  }
+  with_variant(v, static_cast<F &&>(f));
+}
+
 template <int MINB, int PFD, int TMA>
 static void launch_batch_v(int riemann, BatchInst *insts, const int *slots, const int *sb, int n, int total,
                            int grid, cudaStream_t s) {
@@ -1123,6 +1172,8 @@ static cudaError_t configure_rs() {
                                    (int)ring_bytes(P));
       }
     });
+  if (e == cudaSuccess)  // variant 7 (single-grid step only)
+    e = cudaFuncSetAttribute(k_step_f32c<RS, 3, 3, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring_bytes(3));
   return e;
 }
 
@@ -1184,7 +1235,7 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
   const int nsx = (kp.g.nx + OUTW - 1) / OUTW;
   const int nsy = (kp.g.ny + kp.strip_h - 1) / kp.strip_h;
   const int blocks = (nsx * nsy + WPB - 1) / WPB;
-  with_variant(kp.variant, [&](auto minb, auto pfd, auto tma) {
+  with_step_variant(kp.variant, [&](auto minb, auto pfd, auto tma) {
     launch_step_v<decltype(minb)::value, decltype(pfd)::value, decltype(tma)::value>(kp, riemann, blocks, w_in, w_out, tm_in, clk,
                                                                use_clock, host_dt, s);
   });
@@ -1193,7 +1244,7 @@ cudaError_t launch_f32c_step(const KParams32 &kp, int riemann, const float *w_in
 
 // The TMA map of a state array: dimensions (wpitch, jsize, 8 planes), row
 // and plane strides in bytes (multiples of 16: wpitch is a multiple of 4),
-// box 64 x 1 x 8.  The encoder comes from the driver through the runtime's
+// box 64 x 1 x 8 (variant 7: 64 x 2 x 8, two rows per copy).  The encoder comes from the driver through the runtime's
 // versioned entry point (no link against the driver library).
 bool encode_f32c_map(CUtensorMap *map, const float *w, const KParams32 &kp) {
   // looked up once (thread-safe static initialisation); null if unavailable
@@ -1209,7 +1260,7 @@ bool encode_f32c_map(CUtensorMap *map, const float *w, const KParams32 &kp) {
   if ((reinterpret_cast<uintptr_t>(w) & 15u) != 0 || (kp.wpitch & 3) != 0) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)kp.wpitch, (cuuint64_t)kp.g.jsize, 8};
   const cuuint64_t strides[2] = {(cuuint64_t)kp.wpitch * sizeof(float), (cuuint64_t)kp.wplane * sizeof(float)};
-  const cuuint32_t box[3] = {64, 1, 8};
+  const cuuint32_t box[3] = {64, kp.variant == 7 ? 2u : 1u, 8};
   const cuuint32_t estr[3] = {1, 1, 1};
   return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(w), dims, strides, box, estr,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

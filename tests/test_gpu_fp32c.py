@@ -146,13 +146,17 @@ def test_fp32c_nonfinite_state_reports_enumeric(gpu_lib, tmp_path):
 TMA_VARIANT = 6  # rows staged by TMA, waits on mbarriers
 
 
-def test_tma_variant_matches_default(gpu_lib, monkeypatch):
-    """The TMA-staged variant gives the same bits as the default (cp.async)
-    variant on a grid with interior, boundary and ghost-row strips."""
+@pytest.mark.parametrize("variant", [str(TMA_VARIANT), "7"])
+@pytest.mark.parametrize("strip_h", ["16", "64"])
+def test_tma_variant_matches_default(gpu_lib, monkeypatch, variant, strip_h):
+    """The TMA-staged variants -- one row per copy (6) and two rows per copy
+    (7) -- give the same bits as the default (cp.async) variant on a grid
+    with interior, boundary and ghost-row strips."""
     p = e2d.make_params(300, 200, problem="implode", riemann="hllc", gamma0=1.4, cfl=0.8,
                         implode_shape=1, bc=(1, 3, 2, 1), precision=e2d.PRECISION_FP32C)
+    monkeypatch.setenv("E2D_F32C_STRIP_H", strip_h)
     out = []
-    for v in ("4", str(TMA_VARIANT)):
+    for v in ("4", variant):
         monkeypatch.setenv("E2D_F32C_VARIANT", v)
         with e2d.HydroRun(p) as h:
             _, ns, trace = h.step_n(30, 10.0, 0.0, 0)
