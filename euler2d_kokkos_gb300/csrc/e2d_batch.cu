@@ -1,7 +1,8 @@
 // e2d_batch.cu -- batched solves: many independent simulations of uneven
 // size resident in one device memory pool, advanced together by one kernel
-// launch per iteration (k_batch_f32c) with per-instance dt, replayed from
-// CUDA graphs; admission by free pool bytes; strip height per size class and
+// launch per iteration for the FP32C instances (k_batch_f32c) and one for
+// the FP64 ones (k_batch_step_f64) with per-instance dt, replayed from CUDA
+// graphs; admission by free pool bytes; strip height per size class and
 // the kernel's register budget set by a measured autotuner.
 #include "e2d_internal.h"
 
@@ -107,9 +108,10 @@ struct e2d_batch {
   std::vector<int> list;         // slots of the current work list
   int total_strips = 0;
   BatchInst64 *d_insts64 = nullptr;  // slot-indexed FP64 table
-  int *d_list64 = nullptr;           // slots, then fill_begin, then tile_begin (max_inst + 1 each)
+  int *d_list64 = nullptr;           // slots (max_inst), then tile_begin (max_inst + 1)
   std::vector<int> list64;           // slots of the current FP64 work list
-  int total_fill = 0, total_tiles = 0;
+  int total_tiles = 0;
+  int sm_count = 152;  // multiprocessors of the batch's device (the FP64 kernel's persistent grid)
   bool list_dirty = true;
   int grid = 0;
   std::map<int, cudaGraphExec_t> graphs;  // iterations -> graph of the current list
@@ -138,8 +140,8 @@ void drop_graphs(e2d_batch *b) {
 }
 
 size_t inst_bytes(const KParams32 &kp) { return (size_t)2 * 8 * kp.wplane * sizeof(float); }
-// FP64 instance: U, U2 and the primitive array
-size_t inst_bytes64(const KGeom &g) { return (size_t)3 * 4 * g.plane * sizeof(double); }
+// FP64 instance: U, U2 and the primitives of each
+size_t inst_bytes64(const KGeom &g) { return (size_t)4 * 4 * g.plane * sizeof(double); }
 
 int sync_mirrors(e2d_batch *b) {
   std::vector<BatchInst> tmp(b->max_inst);
@@ -160,33 +162,26 @@ int sync_mirrors(e2d_batch *b) {
   return E2D_OK;
 }
 
-// The FP64 work list: used, active FP64 instances with their fill blocks
-// and flux tiles.
+// The FP64 work list: used, active FP64 instances with their tiles.
 int rebuild_list64(e2d_batch *b) {
-  std::vector<int> list, fb, tb;
-  int nf = 0, nt = 0;
+  std::vector<int> list, tb;
+  int nt = 0;
   for (int k = 0; k < b->max_inst; ++k) {
     HostInst &h = b->slots[k];
     if (!h.used || !h.fp64 || !h.mirror64.active) continue;
     list.push_back(k);
-    fb.push_back(nf);
     tb.push_back(nt);
-    nf += h.mirror64.nfill;
     nt += h.mirror64.ntiles;
   }
-  fb.push_back(nf);
   tb.push_back(nt);
   if (!list.empty()) {
     const size_t m = (size_t)b->max_inst;
     B_CK(b, cudaMemcpyAsync(b->d_list64, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, b->stream),
          "list upload");
-    B_CK(b, cudaMemcpyAsync(b->d_list64 + m, fb.data(), sizeof(int) * fb.size(), cudaMemcpyHostToDevice, b->stream),
-         "fill list upload");
-    B_CK(b, cudaMemcpyAsync(b->d_list64 + 2 * m + 1, tb.data(), sizeof(int) * tb.size(), cudaMemcpyHostToDevice,
-                            b->stream), "tile list upload");
+    B_CK(b, cudaMemcpyAsync(b->d_list64 + m, tb.data(), sizeof(int) * tb.size(), cudaMemcpyHostToDevice, b->stream),
+         "tile list upload");
   }
   b->list64 = list;
-  b->total_fill = nf;
   b->total_tiles = nt;
   return E2D_OK;
 }
@@ -263,8 +258,8 @@ int launch_iterations(e2d_batch *b, int iterations) {
         le = launch_batch_f32c(b->riemann, b->variant, b->d_insts, b->d_list, b->d_list + m, (int)b->list.size(),
                                b->total_strips, b->grid, b->stream);
       if (le == cudaSuccess && !b->list64.empty())
-        le = launch_batch_f64(b->riemann, b->d_insts64, b->d_list64, b->d_list64 + m, b->d_list64 + 2 * m + 1,
-                              (int)b->list64.size(), b->total_fill, b->total_tiles, b->stream);
+        le = launch_batch_f64(b->riemann, b->d_insts64, b->d_list64, b->d_list64 + m, (int)b->list64.size(),
+                              b->total_tiles, b->sm_count, b->stream);
     }
     cudaError_t ee = cudaStreamEndCapture(b->stream, &graph);
     if (le != cudaSuccess || ee != cudaSuccess) return berr(b, E2D_ECUDA, "batch capture");
@@ -280,8 +275,9 @@ int launch_iterations(e2d_batch *b, int iterations) {
 }
 
 // An FP64 instance: U (initial state from the host or the device
-// initialiser), U2 = U, the primitive array; bit-identical to the single
-// FP64 path step for step.
+// initialiser), U2 = U, the primitives of each, primed once here (the
+// prologue of the device loop); bit-identical to the single FP64 path step
+// for step.
 int admit64(e2d_batch *b, const e2d_params &p, double t_end, const double *u0, int slot, int *id) {
   KParams64 kp;
   make_kparams(p, &kp);
@@ -290,7 +286,8 @@ int admit64(e2d_batch *b, const e2d_params &p, double t_end, const double *u0, i
   if (!b->alloc.alloc(need, &off)) return berr(b, E2D_ENOMEM, "admit: pool full");
   double *u0d = reinterpret_cast<double *>(b->pool + off);
   double *u1d = u0d + 4 * kp.g.plane;
-  double *qd = u1d + 4 * kp.g.plane;
+  double *q0d = u1d + 4 * kp.g.plane;
+  double *q1d = q0d + 4 * kp.g.plane;
   const size_t state_bytes = sizeof(double) * 4 * (size_t)kp.g.plane;
   auto undo = [&](int st, const char *m) {
     cudaStreamSynchronize(b->stream);
@@ -309,13 +306,16 @@ int admit64(e2d_batch *b, const e2d_params &p, double t_end, const double *u0, i
   I.kp = kp;
   I.u[0] = u0d;
   I.u[1] = u1d;
-  I.q = qd;
+  I.q[0] = q0d;
+  I.q[1] = q1d;
   I.t = 0.0;
   I.t_end = t_end;
   I.active = I.t < I.t_end;
   batch_f64_shape(kp, &I.nbx, &I.nfill, &I.ntx, &I.ntiles);
   HostInst &h = b->slots[slot];
   if (cudaMemcpyAsync(&b->d_insts64[slot], &I, sizeof(I), cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+      launch_batch_prime_f64(&b->d_insts64[slot], I.nfill, b->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&I, &b->d_insts64[slot], sizeof(I), cudaMemcpyDeviceToHost, b->stream) != cudaSuccess ||
       cudaStreamSynchronize(b->stream) != cudaSuccess)
     return undo(E2D_ECUDA, "admit: table upload");
   h.used = true;
@@ -347,13 +347,20 @@ int e2d_batch_create(int riemann, size_t pool_bytes, int max_instances, e2d_batc
     return st;
   };
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(E2D_ECUDA);
+  {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      return fail(E2D_ECUDA);
+    b->sm_count = sms;
+  }
   if (cudaMalloc(&b->pool, pool_bytes) != cudaSuccess) return fail(E2D_ENOMEM);
   b->pool_bytes = pool_bytes;
   b->alloc.reset(pool_bytes);
   if (cudaMalloc(&b->d_insts, sizeof(BatchInst) * (size_t)max_instances) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&b->d_list, sizeof(int) * (2 * (size_t)max_instances + 1)) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMalloc(&b->d_insts64, sizeof(BatchInst64) * (size_t)max_instances) != cudaSuccess) return fail(E2D_ENOMEM);
-  if (cudaMalloc(&b->d_list64, sizeof(int) * (3 * (size_t)max_instances + 2)) != cudaSuccess) return fail(E2D_ENOMEM);
+  if (cudaMalloc(&b->d_list64, sizeof(int) * (2 * (size_t)max_instances + 1)) != cudaSuccess) return fail(E2D_ENOMEM);
   if (cudaMemsetAsync(b->d_insts, 0, sizeof(BatchInst) * (size_t)max_instances, b->stream) != cudaSuccess ||
       cudaMemsetAsync(b->d_insts64, 0, sizeof(BatchInst64) * (size_t)max_instances, b->stream) != cudaSuccess)
     return fail(E2D_ECUDA);

@@ -447,6 +447,70 @@ __device__ __forceinline__ void block_fold(double term, unsigned int flags, unsi
   }
 }
 
+// The fused step's epilogue for the cells of a tile whose fluxes are in
+// shared memory: the conservative update into u_out, the primitives of the
+// new cells into q_out and the running maximum of their CFL terms and flags.
+template <int TX, int TY, int NT, bool FAST>
+__device__ __forceinline__ void step_epilogue(const KParams64 &kp, const double *__restrict__ u_in,
+                                              double *__restrict__ u_out, double *__restrict__ q_out, int i0,
+                                              int j0, double *smem, double &term, unsigned int &flags) {
+  const KGeom &g = kp.g;
+  const KPhys<double> &ph = kp.ph;
+  const TileSmem<TX, TY> sm(smem);
+  for (int k = threadIdx.x; k < TX * TY; k += NT) {
+    const int y = k / TX, x = k - y * TX;
+    const int gi = i0 + 2 + x, gj = j0 + 2 + y;
+    if (gi < g.nx + 2 && gj < g.ny + 2) {
+      const size_t s = (size_t)gi + (size_t)g.isize * gj;
+      double un[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        un[v] = update_var<TX, TY>(sm, v, x, y, u_in[s + v * g.plane]);
+        u_out[s + v * g.plane] = un[v];
+      }
+      double dd, p, ux, uy, rd = 0.0;
+      if (FAST)
+        primitives_fast(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy, rd);
+      else
+        primitives(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy);
+      q_out[s] = dd;
+      q_out[s + g.plane] = p;
+      q_out[s + 2 * g.plane] = ux;
+      q_out[s + 3 * g.plane] = uy;
+      term = fmax(term, FAST ? cfl_term_fast(ph, rd, p, ux, uy) : cfl_term(ph, dd, p, ux, uy));
+      flags |= state_flags(un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV]);
+    }
+  }
+}
+
+// The ghost cells next to a tile -- those whose nearest interior cell is in
+// it -- receive the ghost fill of u_in in both states, read from interior
+// cells of u_in only (no block writes those during a step).
+template <int TX, int TY, int NT>
+__device__ __forceinline__ void ghost_fill_tile(const KGeom &g, double *__restrict__ u_in, double *__restrict__ u_out,
+                                                int i0, int j0, bool lo_x, bool hi_x, bool lo_y, bool hi_y) {
+  if (!(lo_x || hi_x || lo_y || hi_y)) return;
+  const int xa = lo_x ? 0 : i0 + 2, xb = hi_x ? g.isize : i0 + 2 + TX;
+  const int ya = lo_y ? 0 : j0 + 2, yb = hi_y ? g.jsize : j0 + 2 + TY;
+  const int w = xb - xa, n = w * (yb - ya);
+  for (int k = threadIdx.x; k < n; k += NT) {
+    const int j = ya + k / w, i = xa + k % w;
+    if (i >= 2 && i < g.nx + 2 && j >= 2 && j < g.ny + 2) continue;
+    bool fu, fv;
+    const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
+    const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
+    const size_t s = (size_t)si + (size_t)g.isize * sj, d = (size_t)i + (size_t)g.isize * j;
+    double v4[4] = {u_in[s], u_in[s + g.plane], u_in[s + 2 * g.plane], u_in[s + 3 * g.plane]};
+    if (fu) v4[E2D_IU] = -v4[E2D_IU];
+    if (fv) v4[E2D_IV] = -v4[E2D_IV];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      u_in[d + v * g.plane] = v4[v];
+      u_out[d + v * g.plane] = v4[v];
+    }
+  }
+}
+
 template <int TX, int TY>
 __host__ __device__ constexpr unsigned int qtile_bytes() {
   return (unsigned int)(sizeof(double) * 4 * (TX + 4) * (TY + 4));
@@ -527,57 +591,10 @@ __global__ void __launch_bounds__(NT, MINB)
   unsigned int flags = 0;
   if (ok) {
     tile_fluxes<RS, TX, TY, NT, FAST>(ph, s_dt[1], s_dt[2], smem);
-    const TileSmem<TX, TY> sm(smem);
-    for (int k = tid; k < TX * TY; k += NT) {
-      const int y = k / TX, x = k - y * TX;
-      const int gi = i0 + 2 + x, gj = j0 + 2 + y;
-      if (gi < g.nx + 2 && gj < g.ny + 2) {
-        const size_t s = (size_t)gi + (size_t)g.isize * gj;
-        double un[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          un[v] = update_var<TX, TY>(sm, v, x, y, u_in[s + v * g.plane]);
-          u_out[s + v * g.plane] = un[v];
-        }
-        double dd, p, ux, uy, rd = 0.0;
-        if (FAST)
-          primitives_fast(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy, rd);
-        else
-          primitives(ph, un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV], dd, p, ux, uy);
-        q_out[s] = dd;
-        q_out[s + g.plane] = p;
-        q_out[s + 2 * g.plane] = ux;
-        q_out[s + 3 * g.plane] = uy;
-        term = fmax(term, FAST ? cfl_term_fast(ph, rd, p, ux, uy) : cfl_term(ph, dd, p, ux, uy));
-        flags |= state_flags(un[E2D_ID], un[E2D_IP], un[E2D_IU], un[E2D_IV]);
-      }
-    }
+    step_epilogue<TX, TY, NT, FAST>(kp, u_in, u_out, q_out, i0, j0, smem, term, flags);
   }
-
-  // ghost cells next to this tile: those whose nearest interior cell is in it
-  const bool lo_x = bx == 0, hi_x = bx == (int)gridDim.x - 1;
-  const bool lo_y = by == 0, hi_y = by == (int)gridDim.y - 1;
-  if (lo_x || hi_x || lo_y || hi_y) {
-    const int xa = lo_x ? 0 : i0 + 2, xb = hi_x ? g.isize : i0 + 2 + TX;
-    const int ya = lo_y ? 0 : j0 + 2, yb = hi_y ? g.jsize : j0 + 2 + TY;
-    const int w = xb - xa, n = w * (yb - ya);
-    for (int k = tid; k < n; k += NT) {
-      const int j = ya + k / w, i = xa + k % w;
-      if (i >= 2 && i < g.nx + 2 && j >= 2 && j < g.ny + 2) continue;
-      bool fu, fv;
-      const int si = src_lo_hi(i, g.nx, g.bc_xmin, g.bc_xmax, fu);
-      const int sj = src_lo_hi(j, g.ny, g.bc_ymin, g.bc_ymax, fv);
-      const size_t s = (size_t)si + (size_t)g.isize * sj, d = (size_t)i + (size_t)g.isize * j;
-      double v4[4] = {u_in[s], u_in[s + g.plane], u_in[s + 2 * g.plane], u_in[s + 3 * g.plane]};
-      if (fu) v4[E2D_IU] = -v4[E2D_IU];
-      if (fv) v4[E2D_IV] = -v4[E2D_IV];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        u_in[d + v * g.plane] = v4[v];
-        u_out[d + v * g.plane] = v4[v];
-      }
-    }
-  }
+  ghost_fill_tile<TX, TY, NT>(g, u_in, u_out, i0, j0, bx == 0, bx == (int)gridDim.x - 1, by == 0,
+                              by == (int)gridDim.y - 1);
 
   block_fold<NT>(term, flags, &clk->acc[par ^ 1], &clk->status);
 
@@ -617,65 +634,74 @@ __device__ __forceinline__ int list_entry(const int *__restrict__ begin, int n, 
   return lo;
 }
 
-// The fill pass of one iteration for every listed FP64 instance: one block
-// per fill block of an instance (the single-grid k_fill_f64 with the device
-// clock's mode), the CFL maximum into the instance's accumulator.
-__global__ void __launch_bounds__(FILL_BX *FILL_BY)
-    k_batch_fill_f64(BatchInst64 *__restrict__ insts, const int *__restrict__ list_slots,
-                     const int *__restrict__ fill_begin, const int n_inst) {
-  const int k = list_entry(fill_begin, n_inst, blockIdx.x);
-  BatchInst64 &I = insts[list_slots[k]];
-  if (!I.active) return;  // block-uniform
-  const int b = blockIdx.x - fill_begin[k];
-  const int by = b / I.nbx, bx = b - by * I.nbx;
-  const int par = I.par;
+// An admitted FP64 instance's first primitives and CFL maximum (the device
+// loop's prologue): q[0] from u[0], the maximum into acc[0].
+__global__ void __launch_bounds__(FILL_BX *FILL_BY) k_batch_prime_f64(BatchInst64 *__restrict__ I) {
+  const int by = blockIdx.x / I->nbx, bx = blockIdx.x - by * I->nbx;
   double term = 0.0;
   unsigned int flags = 0;
-  fill_cell(I.kp, I.u[par], I.u[par ^ 1], I.q, FILL_WRITE_Q | FILL_GHOSTS_IN | FILL_GHOSTS_OUT | FILL_DT,
-            bx * FILL_BX + threadIdx.x, by * FILL_BY + threadIdx.y, term, flags);
-  fill_reduce(term, flags, &I.acc, &I.status);
+  fill_cell(I->kp, I->u[0], nullptr, I->q[0], FILL_WRITE_Q | FILL_DT, bx * FILL_BX + threadIdx.x,
+            by * FILL_BY + threadIdx.y, term, flags);
+  fill_reduce(term, flags, &I->acc[0], &I->status);
 }
 
-// The flux pass: one 32 x 32 tile per block with its instance's dt; the
-// instance's last tile advances its loop state (src/main.cpp:139-143).
+// One iteration of every listed FP64 instance in one persistent launch: each
+// block takes 32 x 32 tiles from the work list (instance k's tiles are
+// tile_begin[k] .. tile_begin[k+1]-1) and runs the fused step on each with
+// its instance's dt, primitives and ghost cells (tiles gathered, no TMA);
+// the instance's last tile advances its loop state.
 template <int RS>
 __global__ void __launch_bounds__(512, 1)
-    k_batch_flux_f64(BatchInst64 *__restrict__ insts, const int *__restrict__ list_slots,
-                     const int *__restrict__ tile_begin, const int n_inst) {
-  extern __shared__ double smem[];
-  const int k = list_entry(tile_begin, n_inst, blockIdx.x);
-  BatchInst64 &I = insts[list_slots[k]];
-  if (!I.active) return;  // block-uniform
-  const KPhys<double> &ph = I.kp.ph;
+    k_batch_step_f64(BatchInst64 *__restrict__ insts, const int *__restrict__ list_slots,
+                     const int *__restrict__ tile_begin, const int n_inst, const int total_tiles) {
+  extern __shared__ unsigned char smem_raw[];
+  double *smem = reinterpret_cast<double *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
   __shared__ double s_dt[3];
-  if (threadIdx.x == 0) {
-    const double dt = step_dt(ph, I.acc, I.t, I.t_end);
-    s_dt[0] = dt;
-    s_dt[1] = dt / ph.dx;
-    s_dt[2] = dt / ph.dy;
-  }
-  __syncthreads();
-  const int b = blockIdx.x - tile_begin[k];
-  const int by = b / I.ntx, bx = b - by * I.ntx;
-  const int par = I.par;
-  flux_tile<RS, 32, 32, 512>(I.kp, I.q, I.u[par], I.u[par ^ 1], bx, by, s_dt[1], s_dt[2], smem);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned int ticket = atomicAdd(&I.done, 1u);
-    if (ticket == (unsigned)I.ntiles - 1u) {
-      __threadfence();
-      const double dt = s_dt[0];
-      if (!(dt > 0.0) || nonfinite(dt)) I.status |= E2D_FLAG_BAD_DT;
-      I.dt = dt;
-      I.t = I.t + dt;
-      I.nstep = I.nstep + 1;
-      I.par = par ^ 1;
-      I.acc = 0ull;
-      I.done = 0u;
-      I.active = (I.t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
-      __threadfence();
+  const int tid = threadIdx.x;
+  for (int w = blockIdx.x; w < total_tiles; w += gridDim.x) {
+    const int k = list_entry(tile_begin, n_inst, w);
+    BatchInst64 &I = insts[list_slots[k]];
+    if (!I.active) continue;  // block-uniform
+    const KParams64 &kp = I.kp;
+    const int par = I.par;
+    if (tid == 0) {
+      const double dt = step_dt(kp.ph, I.acc[par], I.t, I.t_end);
+      s_dt[0] = dt;
+      s_dt[1] = dt / kp.ph.dx;
+      s_dt[2] = dt / kp.ph.dy;
     }
+    const int b = w - tile_begin[k];
+    const int by = b / I.ntx, bx = b - by * I.ntx;
+    const int nty = I.ntiles / I.ntx;
+    const int i0 = bx * 32, j0 = by * 32;
+    gather_qtile<32, 32, 512>(kp.g, I.q[par], i0, j0, smem);
+    __syncthreads();
+    double term = 0.0;
+    unsigned int flags = 0;
+    tile_fluxes<RS, 32, 32, 512>(kp.ph, s_dt[1], s_dt[2], smem);
+    step_epilogue<32, 32, 512, false>(kp, I.u[par], I.u[par ^ 1], I.q[par ^ 1], i0, j0, smem, term, flags);
+    ghost_fill_tile<32, 32, 512>(kp.g, I.u[par], I.u[par ^ 1], i0, j0, bx == 0, bx == I.ntx - 1, by == 0,
+                                 by == nty - 1);
+    block_fold<512>(term, flags, &I.acc[par ^ 1], &I.status);
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      const unsigned int ticket = atomicAdd(&I.done, 1u);
+      if (ticket == (unsigned)I.ntiles - 1u) {
+        __threadfence();
+        const double dt = s_dt[0];
+        if (!(dt > 0.0) || nonfinite(dt)) I.status |= E2D_FLAG_BAD_DT;
+        I.dt = dt;
+        I.t = I.t + dt;
+        I.nstep = I.nstep + 1;
+        I.par = par ^ 1;
+        I.acc[par] = 0ull;  // read by this step; folded into by the next
+        I.done = 0u;
+        I.active = (I.t < I.t_end) && !(I.status & (E2D_FLAG_NONFINITE | E2D_FLAG_BAD_DT));
+        __threadfence();
+      }
+    }
+    __syncthreads();  // s_dt and the shared tile are rewritten by the next tile
   }
 }
 
@@ -866,8 +892,8 @@ static cudaError_t configure_rs() {
 
 template <int RS>
 static cudaError_t set_batch_flux_smem() {
-  return cudaFuncSetAttribute(k_batch_flux_f64<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)flux_smem_bytes<32, 32>());
+  return cudaFuncSetAttribute(k_batch_step_f64<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)step_smem_bytes<32, 32>());
 }
 
 cudaError_t configure_f64_kernels() {
@@ -887,20 +913,25 @@ void batch_f64_shape(const KParams64 &kp, int *nbx, int *nfill, int *ntx, int *n
   *ntiles = *ntx * ((kp.g.ny + 31) / 32);
 }
 
-cudaError_t launch_batch_f64(int riemann, BatchInst64 *insts, const int *list_slots, const int *fill_begin,
-                             const int *tile_begin, int n_inst, int total_fill, int total_tiles, cudaStream_t s) {
-  if (n_inst <= 0 || total_fill <= 0 || total_tiles <= 0) return cudaSuccess;
-  k_batch_fill_f64<<<total_fill, dim3(FILL_BX, FILL_BY), 0, s>>>(insts, list_slots, fill_begin, n_inst);
-  const size_t sm = flux_smem_bytes<32, 32>();
+cudaError_t launch_batch_prime_f64(BatchInst64 *inst, int nfill, cudaStream_t s) {
+  k_batch_prime_f64<<<nfill, dim3(FILL_BX, FILL_BY), 0, s>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_f64(int riemann, BatchInst64 *insts, const int *list_slots, const int *tile_begin,
+                             int n_inst, int total_tiles, int grid_blocks, cudaStream_t s) {
+  if (n_inst <= 0 || total_tiles <= 0) return cudaSuccess;
+  const size_t sm = step_smem_bytes<32, 32>();
+  const int grid = grid_blocks < total_tiles ? grid_blocks : total_tiles;
   switch (riemann) {
     case E2D_RIEMANN_HLLC:
-      k_batch_flux_f64<E2D_RIEMANN_HLLC><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      k_batch_step_f64<E2D_RIEMANN_HLLC><<<grid, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst, total_tiles);
       break;
     case E2D_RIEMANN_HLL:
-      k_batch_flux_f64<E2D_RIEMANN_HLL><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      k_batch_step_f64<E2D_RIEMANN_HLL><<<grid, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst, total_tiles);
       break;
     default:
-      k_batch_flux_f64<E2D_RIEMANN_APPROX><<<total_tiles, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst);
+      k_batch_step_f64<E2D_RIEMANN_APPROX><<<grid, 512, sm, s>>>(insts, list_slots, tile_begin, n_inst, total_tiles);
       break;
   }
   return cudaGetLastError();

@@ -196,28 +196,32 @@ struct BatchInst {
   unsigned int status;          // E2D_FLAG_* bits
 };
 
-// An FP64 instance of a batch: the reference's two states and the primitive
-// array in the pool, stepped by k_batch_fill_f64 + k_batch_flux_f64.
+// An FP64 instance of a batch: the reference's two states and the
+// primitives of each in the pool, stepped by the fused step
+// (k_batch_step_f64) after one prologue at admission (k_batch_prime_f64).
 struct BatchInst64 {
   KParams64 kp;
   double *u[2];
-  double *q;
-  double t, t_end, dt;       // dt: of the last step taken
-  unsigned long long acc;    // CFL maximum of the current step (fill pass)
-  int par;                   // u[par] holds the current state
-  int active;                // 1 while t < t_end
+  double *q[2];                  // q[par]: primitives of u[par] (interior cells)
+  double t, t_end, dt;           // dt: of the last step taken
+  unsigned long long acc[2];     // CFL maxima by step parity (the step of parity n reads acc[n & 1])
+  int par;                       // u[par] holds the current state
+  int active;                    // 1 while t < t_end
   int nstep;
-  int nbx, nfill;            // fill blocks per row, total
-  int ntx, ntiles;           // flux tiles per row, total
-  unsigned int done;         // flux tiles finished in the current iteration
-  unsigned int status;       // E2D_FLAG_* bits
+  int nbx, nfill;                // prologue blocks per row, total
+  int ntx, ntiles;               // 32 x 32 tiles per row, total
+  unsigned int done;             // tiles finished in the current iteration
+  unsigned int status;           // E2D_FLAG_* bits
 };
 
-// One FP64 iteration of every listed FP64 instance: list entry k is table
-// slot list_slots[k]; fill_begin[k] / tile_begin[k] are its first global fill
-// block / flux tile (n_inst + 1 entries each, the last = the totals).
-cudaError_t launch_batch_f64(int riemann, BatchInst64 *insts, const int *list_slots, const int *fill_begin,
-                             const int *tile_begin, int n_inst, int total_fill, int total_tiles, cudaStream_t s);
+// The prologue of a newly admitted FP64 instance (q[0], acc[0] from u[0]).
+cudaError_t launch_batch_prime_f64(BatchInst64 *inst, int nfill, cudaStream_t s);
+// One FP64 iteration of every listed FP64 instance in one persistent launch
+// of at most grid_blocks blocks: list entry k is table slot list_slots[k];
+// tile_begin[k] is its first global tile (n_inst + 1 entries, the last =
+// total_tiles).
+cudaError_t launch_batch_f64(int riemann, BatchInst64 *insts, const int *list_slots, const int *tile_begin,
+                             int n_inst, int total_tiles, int grid_blocks, cudaStream_t s);
 // Fill blocks and flux tiles of an FP64 instance.
 void batch_f64_shape(const KParams64 &kp, int *nbx, int *nfill, int *ntx, int *ntiles);
 

@@ -244,9 +244,10 @@ int e2d_step_n(e2d_sim *sim, int n, double t_end, double *t, int *nStep, double 
  * Batched solves.  No counterpart in the reference, which runs one grid per
  * process: the serving mode here keeps many independent simulations of
  * uneven size resident in one device memory pool and advances all active
- * ones together, one kernel launch per iteration for the FP32C instances and
- * one fill + flux pair for the FP64 ones (each instance with its own dt and
- * t_end), replayed from CUDA graphs.  Arithmetic: each instance's
+ * ones together, one persistent kernel launch per iteration for the FP32C
+ * instances and one for the FP64 ones (the fused step over a tile
+ * work-list; each instance with its own dt and t_end), replayed from CUDA
+ * graphs.  Arithmetic: each instance's
  * params.precision (FP64 instances end bit for bit where the single FP64
  * path ends).  One Riemann solver per batch.  A handle is used from one host
  * thread.

@@ -200,7 +200,7 @@ def test_batch_instance_bytes_is_the_admission_arithmetic():
     """Pool bytes one admission takes (host arithmetic, no device): FP32C,
     two states of 8 float planes with the row pitch padded to 4 floats plus
     the FP64 staging array of the initial state; FP64, U, U2 and the
-    primitive array; each rounded to the pool's 256-byte blocks.  Invalid
+    primitives of each; each rounded to the pool's 256-byte blocks.  Invalid
     parameters give 0."""
     rnd = lambda b: (b + 255) // 256 * 256
     for nx, ny in [(64, 64), (100, 37), (1024, 512), (2, 2)]:
@@ -209,7 +209,7 @@ def test_batch_instance_bytes_is_the_admission_arithmetic():
         p32 = e2d.make_params(nx, ny, precision=e2d.PRECISION_FP32C)
         assert e2d.Batch.instance_bytes(p32) == rnd(2 * 8 * pitch * jsize * 4) + rnd(4 * isize * jsize * 8)
         p64 = e2d.make_params(nx, ny, precision=e2d.PRECISION_FP64)
-        assert e2d.Batch.instance_bytes(p64) == rnd(3 * 4 * isize * jsize * 8)
+        assert e2d.Batch.instance_bytes(p64) == rnd(4 * 4 * isize * jsize * 8)
     bad = e2d.make_params(16, 16)
     bad.cfl = 0.0
     assert e2d.Batch.instance_bytes(bad) == 0
