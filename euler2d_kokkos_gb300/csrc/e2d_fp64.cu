@@ -236,13 +236,27 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
   double *sXm = sm.sXm, *sXp = sm.sXp, *sYm = sm.sYm, *sYp = sm.sYp;
   const int tid = threadIdx.x;
 
-  // stage 2: slopes, trace sources and face states
+  // stage 2: slopes, trace sources and face states.  Items enumerate the
+  // tile and its 1-cell ring without the ring's four corners (which carry no
+  // face), so the last partial round of 32 x 32 tiles is 4 whole warps -- one
+  // per scheduler -- instead of 4 warps and 4 threads.
   const int st_kind = (ph.slope_type == 2.0) ? 2 : (ph.slope_type == 1.0) ? 1 : 0;
-  for (int k = tid; k < YH * XW; k += NT) {
-    const int yy = k / XW, xx = k - yy * XW;  // cell (xx-1, yy-1) of the tile
+  constexpr int NS2 = YH * XW - 4;
+  for (int k = tid; k < NS2; k += NT) {
+    int yy, xx;  // cell (xx-1, yy-1) of the tile
+    if (k < TX) {
+      yy = 0;
+      xx = k + 1;
+    } else if (k < TX + TY * XW) {
+      const int r = k - TX;
+      yy = 1 + r / XW;
+      xx = r - (yy - 1) * XW;
+    } else {
+      yy = YH - 1;
+      xx = k - (TX + TY * XW) + 1;
+    }
     const bool xin = (xx >= 1) && (xx <= TX);
     const bool yin = (yy >= 1) && (yy <= TY);
-    if (!xin && !yin) continue;
     const int c = (yy + 1) * QW + (xx + 1);
     double qc[4], dqx[4], dqy[4];
 #pragma unroll
