@@ -4,8 +4,9 @@
 //
 // The device time loop runs one fused launch per step (k_step_f64, after a
 // prologue k_fill_f64 that folds the first step's CFL maximum and writes the
-// primitives of the initial state).  The host-driven godunov_unsplit and the
-// batches run the same step as two launches:
+// primitives of the initial state); FP64 batch instances run the same fused
+// step in one persistent launch per iteration (k_batch_step_f64).  The
+// host-driven godunov_unsplit runs it as two launches:
 //   k_fill_f64         ghost fill (make_boundaries, src/HydroRun.h:388-399)
 //                      into both states, primitives of every cell
 //                      (ConvertToPrimitivesFunctor, src/HydroRunFunctors.h:84-143)
@@ -239,7 +240,9 @@ __device__ __forceinline__ void tile_fluxes(const KPhys<double> &ph, const doubl
   // stage 2: slopes, trace sources and face states.  Items enumerate the
   // tile and its 1-cell ring without the ring's four corners (which carry no
   // face), so the last partial round of 32 x 32 tiles is 4 whole warps -- one
-  // per scheduler -- instead of 4 warps and 4 threads.
+  // per scheduler -- instead of 4 warps and 4 threads.  The FP64 pipe takes
+  // as long for a warp instruction with a few active lanes as for a full
+  // one, so a partial round costs what its busiest scheduler's warps cost.
   const int st_kind = (ph.slope_type == 2.0) ? 2 : (ph.slope_type == 1.0) ? 1 : 0;
   constexpr int NS2 = YH * XW - 4;
   for (int k = tid; k < NS2; k += NT) {
