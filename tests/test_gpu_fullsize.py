@@ -1,8 +1,8 @@
 """The benchmark configurations at their full sizes on the GPU.
 
-- C2, the 4096x4096 blast (FP64, HLLC): 20 steps bit for bit against the
-  oracle (whose restatement is bit-identical to the reference on every golden
-  case), run on the host's cores with OpenMP;
+- C2, the 4096x4096 blast (FP64, HLLC and HLL): its 200 steps bit for bit
+  against the oracle (whose restatement is bit-identical to the reference on
+  every golden case), run on the host's cores with OpenMP;
 - size-independent properties at 4096^2: mass and energy conservation with
   reflecting walls, and the x <-> y mirror symmetry of the centred blast;
 - C3, the 8192x8192 four-quadrant problem: FP32C against the FP64 path after
@@ -27,17 +27,18 @@ def run(h, nsteps, t_end=10.0):
     return h.current(ns), tr
 
 
-def test_c2_blast_4096_bitwise_vs_oracle(gpu_lib, tmp_path):
-    text = C.ini_text(4096, 4096, problem="blast", extra=BLAST_INI)
+@pytest.mark.parametrize("riemann", ["hllc", "hll"])
+def test_c2_blast_4096_bitwise_vs_oracle(gpu_lib, tmp_path, riemann):
+    text = C.ini_text(4096, 4096, problem="blast", riemann=riemann, extra=BLAST_INI)
     p = e2d.HydroParams.from_ini(C.write_ini(text, str(tmp_path)))
     with e2d.HydroRun(p) as h:
         u0 = h.U
-        u, dts = run(h, 20, C.f32(10.0))
+        u, dts = run(h, 200, C.f32(10.0))
     op = po.make_params(**C.oracle_kwargs(text))
     # the device initialiser (ini reals rounded through float, as ConfigMap does)
     assert np.array_equal(u0, po.init_blast(op, p_out=C.f32(0.1)))
-    uo, dto, _, no = po.run(op, u0, 20, C.f32(10.0))
-    assert no == 20
+    uo, dto, _, no = po.run(op, u0, 200, C.f32(10.0))
+    assert no == 200
     assert np.array_equal(dts, dto)
     assert np.array_equal(u, uo)
 
