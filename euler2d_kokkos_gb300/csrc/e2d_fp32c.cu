@@ -3,9 +3,11 @@
 // The state keeps each conserved variable as an unevaluated sum hi + lo of
 // two floats (~48 significant bits), so the small flux increments of a step
 // are not rounded away; slopes, traces and Riemann fluxes are computed in FP32
-// from hi.  The update adds the flux balance with TwoSum (Knuth, "The Art of
-// Computer Programming" vol. 2, 4.2.2) and renormalises with Fast2Sum
-// (Dekker, 1971).  The CFL maximum stays FP64: each warp selects its largest
+// from hi.  The update adds the flux balance du to the low word (one FP32
+// rounding, 2^-24 |du|: the size of du's own FP32 rounding) and renormalises
+// the pair with Fast2Sum (Dekker, 1971), exact while |hi| >= |lo + du|; where
+// a value crosses zero the pair keeps the correctly rounded sum, the accuracy
+// of a plain FP32 update for that step.  The CFL maximum stays FP64: each warp selects its largest
 // FP32 wave-speed term and, unless it is clearly below the running maximum,
 // recomputes that cell's term in FP64 from hi + lo; warps combine with an
 // FP64 max.
@@ -806,13 +808,9 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
           // +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
           const float2 du = (fxl[v] - fx_prev[v]) + (fy_prev[v] - fy[v]);
           const float2 hi = uhi[v];
-          float2 lo = ulo[v];
-          const float2 sum = hi + du;           // TwoSum(hi, du)
-          const float2 bb = sum - hi;
-          const float2 err = (hi - (sum - bb)) + (du - bb);
-          lo = lo + err;
-          const float2 h2 = sum + lo;           // Fast2Sum(sum, lo)
-          const float2 l2 = lo - (h2 - sum);
+          const float2 tl = ulo[v] + du;        // the low word takes the update
+          const float2 h2 = hi + tl;            // Fast2Sum(hi, tl)
+          const float2 l2 = tl - (h2 - hi);
           *reinterpret_cast<float2 *>(w_out + base + v * kp.wplane) = h2;
           *reinterpret_cast<float2 *>(w_out + base + (4 + v) * kp.wplane) = l2;
           nh[v] = h2;
