@@ -66,6 +66,7 @@ __device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
 // Constants broadcast to both halves of a float2.
 struct C2 {
   float2 half, mhalf, smallr, smallp, smallc2, gamma0, gm1, entho, st;
+  float2 ggm1, gsmallp;  // gamma (gamma - 1), gamma smallp
 };
 
 __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
@@ -79,6 +80,8 @@ __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
   k.gm1 = f2(ph.gm1);
   k.entho = f2(ph.entho);
   k.st = f2(ph.slope_type);
+  k.ggm1 = f2(ph.gamma0 * ph.gm1);
+  k.gsmallp = f2(ph.gamma0 * ph.smallp);
   return k;
 }
 
@@ -278,10 +281,14 @@ __device__ __forceinline__ double cfl_term64(const KPhys<double> &ph, double rho
 
 // The CFL term of two cells from their conserved values; idx = (1/dx, 1/dy).
 __device__ __forceinline__ float2 cfl_term2(const C2 &k, float2 idx, const float2 u[4]) {
-  float2 q[4];
-  prims2(k, u[0], u[1], u[2], u[3], q);
-  const float2 c = sqrt2(k.gamma0 * q[E2D_IP] * rcp2(q[E2D_ID]));
-  return fma2(c + abs2(q[E2D_IU]), f2(idx.x), (c + abs2(q[E2D_IV])) * f2(idx.y));
+  // the primitives' u, v and internal energy e/d - (u^2+v^2)/2; the sound
+  // speed from gamma p / d = gamma max((gamma-1) ei, smallp), p's cut-off
+  // divided through by d
+  const float2 inv = rcp2(max2(u[0], k.smallr));
+  const float2 ux = u[2] * inv, uy = u[3] * inv;
+  const float2 ei = fma2(u[1], inv, k.mhalf * fma2(ux, ux, uy * uy));
+  const float2 c = sqrt2(max2(k.ggm1 * ei, k.gsmallp));
+  return fma2(c + abs2(ux), f2(idx.x), (c + abs2(uy)) * f2(idx.y));
 }
 
 // Folds one candidate's FP64 CFL term into *target -- skipped when its FP32
@@ -758,19 +765,20 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     // m, so the solves of iteration rb-1 (and the x-solve of row re) are
     // never read.
     float2 xl[4], xr[4], ymin[4], ymax[4];
-    // q -/+ dq/2 as one FMA each (the halving is exact), the source term
-    // as ns0 * (-dt/(2dx)): the same values as (q -/+ dq*0.5) + s0*0.5*dt/dx
+    // the source term first, ns0 * (-dt/(2dx)) added to q by one FMA, then
+    // -/+ dq/2 by one FMA each (the halving is exact): the reference's
+    // (q -/+ dq*0.5) + s0*0.5*dt/dx summed in another order
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const float2 sx_ = ns0[v] * hdtdx;
-      float2 xmin = fma2(dqx[v], k.mhalf, qb[v]) + sx_;
-      float2 xmax = fma2(dqx[v], k.half, qb[v]) + sx_;
+      const float2 bx = fma2(ns0[v], hdtdx, qb[v]);  // q + s0 dt/(2dx)
+      float2 xmin = fma2(dqx[v], k.mhalf, bx);
+      float2 xmax = fma2(dqx[v], k.half, bx);
       if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
       xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
       xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
-      const float2 sy_ = ns0[v] * hdtdy;
-      ymin[v] = fma2(dqy[v], k.mhalf, qb[v]) + sy_;
-      ymax[v] = fma2(dqy[v], k.half, qb[v]) + sy_;
+      const float2 by = fma2(ns0[v], hdtdy, qb[v]);  // q + s0 dt/(2dy)
+      ymin[v] = fma2(dqy[v], k.mhalf, by);
+      ymax[v] = fma2(dqy[v], k.half, by);
     }
     ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
     ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
@@ -782,12 +790,11 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
       float2 f[4];
       riemann2<RS>(ph, k, xl, xr, fx);
       riemann2<RS>(ph, k, yl, yr, f);
-#pragma unroll
-      for (int v = 0; v < 4; ++v) fx[v] = fx[v] * dtdx;
-      fy[E2D_ID] = f[E2D_ID] * dtdy;
-      fy[E2D_IP] = f[E2D_IP] * dtdy;
-      fy[E2D_IU] = f[E2D_IV] * dtdy;
-      fy[E2D_IV] = f[E2D_IU] * dtdy;
+      // unscaled: dt/dx and dt/dy are applied in the update
+      fy[E2D_ID] = f[E2D_ID];
+      fy[E2D_IP] = f[E2D_IP];
+      fy[E2D_IU] = f[E2D_IV];
+      fy[E2D_IV] = f[E2D_IU];
     }
     // compensated update of row m-1
     if (m >= rb + 1) {
@@ -809,7 +816,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
           // +Fx(i) -Fx(i+1) +Fy(j) -Fy(j+1)
-          const float2 du = (fxl[v] - fx_prev[v]) + (fy_prev[v] - fy[v]);
+          const float2 du = fma2(fxl[v] - fx_prev[v], dtdx, (fy_prev[v] - fy[v]) * dtdy);
           const float2 hi = uhi[v];
           const float2 tl = ulo[v] + du;        // the low word takes the update
           const float2 h2 = hi + tl;            // Fast2Sum(hi, tl)
