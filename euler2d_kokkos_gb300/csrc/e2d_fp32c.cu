@@ -67,6 +67,7 @@ __device__ __forceinline__ float2 sel2(bool cx, bool cy, float2 a, float2 b) {
 struct C2 {
   float2 half, mhalf, smallr, smallp, smallc2, gamma0, gm1, entho, st;
   float2 ggm1, gsmallp;  // gamma (gamma - 1), gamma smallp
+  float2 h2st, hst, mhst;  // 1 / (2 slope_type), slope_type / 2, -slope_type / 2
 };
 
 __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
@@ -82,6 +83,9 @@ __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
   k.st = f2(ph.slope_type);
   k.ggm1 = f2(ph.gamma0 * ph.gm1);
   k.gsmallp = f2(ph.gamma0 * ph.smallp);
+  k.h2st = f2(ph.slope_type > 0.0f ? 0.5f / ph.slope_type : 0.0f);
+  k.hst = f2(0.5f * ph.slope_type);
+  k.mhst = f2(-0.5f * ph.slope_type);
   return k;
 }
 
@@ -123,8 +127,11 @@ __device__ __forceinline__ float2 minmod2(float2 a, float2 b, float2 c) {
   const float2 hi = make_float2(max3f(a.x, b.x, c.x), max3f(a.y, b.y, c.y));
   return max2(lo, f2(0.0f)) + min2(hi, f2(0.0f));
 }
+// The slope divided by slope_type: minmod is homogeneous, so
+// minmod(st a, st b, c) = st minmod(a, b, c / st); the callers carry the
+// factor st in their constants (exact for slope_type 1 and 2).
 __device__ __forceinline__ float2 slope2(const C2 &k, float2 q, float2 qp, float2 qm) {
-  return minmod2(k.st * (q - qm), k.st * (qp - q), k.half * (qp - qm));
+  return minmod2(q - qm, qp - q, k.h2st * (qp - qm));
 }
 
 // riemann_hllc (src/HydroBaseFunctor.h:704-809) for two faces.
@@ -132,8 +139,6 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
   const float2 rl = max2(ql[E2D_ID], k.smallr), rr = max2(qr[E2D_ID], k.smallr);
   const float2 pl = max2(ql[E2D_IP], rl * k.smallp), pr = max2(qr[E2D_IP], rr * k.smallp);
   const float2 ul = ql[E2D_IU], ur = qr[E2D_IU], vl = ql[E2D_IV], vr = qr[E2D_IV];
-  const float2 etotl = fma2(pl, k.entho, k.half * rl * fma2(ul, ul, vl * vl));
-  const float2 etotr = fma2(pr, k.entho, k.half * rr * fma2(ur, ur, vr * vr));
   const float2 cl = sqrt2(max2(k.gamma0 * pl * rcp2(rl), k.smallc2));
   const float2 cr = sqrt2(max2(k.gamma0 * pr * rcp2(rr), k.smallc2));
   const float2 cmax = max2(cl, cr);
@@ -147,7 +152,9 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
   const bool lx = ustar.x > 0.0f, ly = ustar.y > 0.0f;
   const float2 S = sel2(lx, ly, SL, SR);
   const float2 rs = sel2(lx, ly, rl, rr), us = sel2(lx, ly, ul, ur), ps = sel2(lx, ly, pl, pr);
-  const float2 es = sel2(lx, ly, etotl, etotr);
+  const float2 vs = sel2(lx, ly, vl, vr);
+  // the total energy of the contact's side only (the other is never read)
+  const float2 es = fma2(ps, k.entho, k.half * rs * fma2(us, us, vs * vs));
   const float2 sdu = S - us;
   const float2 isds = rcp2(S - ustar);
   const float2 rstar = rs * sdu * isds;
@@ -560,6 +567,8 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
   const int st_kind = (ph.slope_type == 2.0f) ? 2 : (ph.slope_type == 1.0f) ? 1 : 0;
   const float2 hdtdx = k.mhalf * dtdx, hdtdy = k.mhalf * dtdy;  // exact halvings
+  // the same for slopes divided by slope_type (slope2)
+  const float2 hdtdxs = hdtdx * k.st, hdtdys = hdtdy * k.st;
 
   float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
   float2 ymax_prev[4];  // YMAX states of row m-1
@@ -744,9 +753,10 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
         dqy[v] = slope2(k, qb[v], qc[v], qa[v]);
       }
     }
-    // trace sources (src/HydroBaseFunctor.h:246-249), negated: ns0 = -s0,
-    // and the half-step terms below take -1/2 (exact: the sign is the only
-    // difference)
+    // trace sources (src/HydroBaseFunctor.h:246-249), negated and divided
+    // by slope_type like the slopes: ns0 = -s0 / st; the half-step terms
+    // below take -st/2 (exact for slope_type 1 and 2: a sign and a power of
+    // two)
     float2 ns0[4];
     {
       const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
@@ -770,15 +780,15 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     // (q -/+ dq*0.5) + s0*0.5*dt/dx summed in another order
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const float2 bx = fma2(ns0[v], hdtdx, qb[v]);  // q + s0 dt/(2dx)
-      float2 xmin = fma2(dqx[v], k.mhalf, bx);
-      float2 xmax = fma2(dqx[v], k.half, bx);
+      const float2 bx = fma2(ns0[v], hdtdxs, qb[v]);  // q + s0 dt/(2dx)
+      float2 xmin = fma2(dqx[v], k.mhst, bx);
+      float2 xmax = fma2(dqx[v], k.hst, bx);
       if (v == E2D_ID) xmin = max2(xmin, k.smallr), xmax = max2(xmax, k.smallr);
       xl[v] = xmax;  // left states of faces (c0|c1) and (c1|c1+1)
       xr[v] = make_float2(xmin.y, __shfl_down_sync(0xffffffffu, xmin.x, 1));
-      const float2 by = fma2(ns0[v], hdtdy, qb[v]);  // q + s0 dt/(2dy)
-      ymin[v] = fma2(dqy[v], k.mhalf, by);
-      ymax[v] = fma2(dqy[v], k.half, by);
+      const float2 by = fma2(ns0[v], hdtdys, qb[v]);  // q + s0 dt/(2dy)
+      ymin[v] = fma2(dqy[v], k.mhst, by);
+      ymax[v] = fma2(dqy[v], k.hst, by);
     }
     ymin[E2D_ID] = max2(ymin[E2D_ID], k.smallr);
     ymax[E2D_ID] = max2(ymax[E2D_ID], k.smallr);
