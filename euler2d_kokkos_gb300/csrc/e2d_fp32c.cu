@@ -848,8 +848,9 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
           if (t.y > best && c0 + 1 < g.nx + 2) best = t.y, blocal = loc + 1;
         }
       }
-      const int r = m - 1;
-      if (target && (((r - 2) % CFL_UNIT_ROWS) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
+      const int r = m - 1;  // >= rb >= 2, so the low bits of r - 2 are its remainder
+      static_assert((CFL_UNIT_ROWS & (CFL_UNIT_ROWS - 1)) == 0, "fold units are a power of two rows");
+      if (target && (((r - 2) & (CFL_UNIT_ROWS - 1)) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
         float ut;
         const int win = unit_argmax(best, blocal, &ut);
         if (lane == unit) pend_term = ut, pend_local = win;
