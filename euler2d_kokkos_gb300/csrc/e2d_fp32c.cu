@@ -89,17 +89,23 @@ __device__ __forceinline__ C2 make_c2(const KPhys<float> &ph) {
   return k;
 }
 
-// computePrimitives (src/HydroBaseFunctor.h:76-102) for two cells.
+// computePrimitives (src/HydroBaseFunctor.h:76-102) for two cells; `inv`
+// receives 1 / d, which the trace reuses.
 __device__ __forceinline__ void prims2(const C2 &k, float2 rho, float2 e, float2 mx, float2 my,
-                                       float2 q[4]) {
+                                       float2 q[4], float2 &inv) {
   const float2 d = max2(rho, k.smallr);
-  const float2 inv = rcp2(d);
+  inv = rcp2(d);
   const float2 u = mx * inv, v = my * inv;
   const float2 ei = fma2(e, inv, k.mhalf * fma2(u, u, v * v));  // e/d - (u^2+v^2)/2
   q[E2D_ID] = d;
   q[E2D_IP] = max2(k.gm1 * d * ei, d * k.smallp);
   q[E2D_IU] = u;
   q[E2D_IV] = v;
+}
+__device__ __forceinline__ void prims2(const C2 &k, float2 rho, float2 e, float2 mx, float2 my,
+                                       float2 q[4]) {
+  float2 inv;
+  prims2(k, rho, e, mx, my, q, inv);
 }
 
 // Three-input minimum and maximum (one instruction each on sm_100 and later).
@@ -135,8 +141,10 @@ __device__ __forceinline__ float2 slope2(const C2 &k, float2 q, float2 qp, float
 }
 
 // riemann_hllc (src/HydroBaseFunctor.h:704-809) for two faces.
+// The face states' densities arrive clamped to smallr by the trace, so the
+// reference's clamp here would return them unchanged.
 __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const float2 qr[4], float2 f[4]) {
-  const float2 rl = max2(ql[E2D_ID], k.smallr), rr = max2(qr[E2D_ID], k.smallr);
+  const float2 rl = ql[E2D_ID], rr = qr[E2D_ID];
   const float2 pl = max2(ql[E2D_IP], rl * k.smallp), pr = max2(qr[E2D_IP], rr * k.smallp);
   const float2 ul = ql[E2D_IU], ur = qr[E2D_IU], vl = ql[E2D_IV], vr = qr[E2D_IV];
   const float2 cl = sqrt2(max2(k.gamma0 * pl * rcp2(rl), k.smallc2));
@@ -180,7 +188,7 @@ __device__ __forceinline__ void hllc2(const C2 &k, const float2 ql[4], const flo
 
 // HLL flux (Toro eq. 10.21, riemann_hllc's wave speeds) for two faces.
 __device__ __forceinline__ void hll2(const C2 &k, const float2 ql[4], const float2 qr[4], float2 f[4]) {
-  const float2 rl = max2(ql[E2D_ID], k.smallr), rr = max2(qr[E2D_ID], k.smallr);
+  const float2 rl = ql[E2D_ID], rr = qr[E2D_ID];  // clamped by the trace (hllc2)
   const float2 pl = max2(ql[E2D_IP], rl * k.smallp), pr = max2(qr[E2D_IP], rr * k.smallp);
   const float2 ul = ql[E2D_IU], ur = qr[E2D_IU], vl = ql[E2D_IV], vr = qr[E2D_IV];
   const float2 etotl = fma2(pl, k.entho, k.half * rl * fma2(ul, ul, vl * vl));
@@ -571,6 +579,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   const float2 hdtdxs = hdtdx * k.st, hdtdys = hdtdy * k.st;
 
   float2 qa[4], qb[4];  // primitives of rows m-1 and m (m: row whose faces are built next)
+  float2 ib;            // 1 / density of row m (from its primitives)
   float2 ymax_prev[4];  // YMAX states of row m-1
   float2 fx_prev[4];    // x-fluxes of row m-1: .x face (c0|c1), .y face (c1|c1+1)
   float2 fy_prev[4];    // y-flux of the face between rows m-2 and m-1
@@ -678,13 +687,13 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     staged_hi(rb - 2, 0, u);
     prims2(k, u[0], u[1], u[2], u[3], qa);
     staged_hi(rb - 1, 1, u);
-    prims2(k, u[0], u[1], u[2], u[3], qb);
+    prims2(k, u[0], u[1], u[2], u[3], qb, ib);
   } else {
     float2 u[4];
     load_row(kp, w_in, rb - 2, c0, direct, u);
     prims2(k, u[0], u[1], u[2], u[3], qa);
     load_row(kp, w_in, rb - 1, c0, direct, u);
-    prims2(k, u[0], u[1], u[2], u[3], qb);
+    prims2(k, u[0], u[1], u[2], u[3], qb, ib);
     load_row(kp, w_in, rb, c0, direct, pf);
   }
   // march: row n = m + 1 is loaded; faces of row m built; y-flux of face
@@ -693,7 +702,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   // (measured 0.75 % faster at 8192^2 than the rolled loop)
 #pragma unroll 2
   for (int m = rb - 1; m <= re; ++m) {
-    float2 qc[4];
+    float2 qc[4], ic;
     if ((PFD > 0)) {
       // wait for row m+1 (rows m+2 .. m+PFD may still be in flight); the
       // barrier makes every lane's copies visible to the warp and orders
@@ -721,12 +730,12 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
       }
       float2 u[4];
       staged_hi(m + 1, wrap(sm1 + 2), u);
-      prims2(k, u[0], u[1], u[2], u[3], qc);
+      prims2(k, u[0], u[1], u[2], u[3], qc, ic);
     } else {
       float2 u[4] = {pf[0], pf[1], pf[2], pf[3]};
       // issue the next row's loads before this row's arithmetic
       if (m + 2 <= re + 1) load_row(kp, w_in, m + 2, c0, direct, pf);
-      prims2(k, u[0], u[1], u[2], u[3], qc);
+      prims2(k, u[0], u[1], u[2], u[3], qc, ic);
     }
     // the update of row m-1 reads its (hi, lo): issue those loads early too
     const bool upd = (m >= rb + 1) && writer;
@@ -761,7 +770,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     {
       const float2 r = qb[E2D_ID], p = qb[E2D_IP], u = qb[E2D_IU], v = qb[E2D_IV];
       const float2 div = dqx[E2D_IU] + dqy[E2D_IV];
-      const float2 ir = rcp2(r);
+      const float2 ir = ib;
       ns0[E2D_ID] = fma2(u, dqx[E2D_ID], fma2(v, dqy[E2D_ID], div * r));
       ns0[E2D_IP] = fma2(u, dqx[E2D_IP], fma2(v, dqy[E2D_IP], div * k.gamma0 * p));
       ns0[E2D_IU] = fma2(u, dqx[E2D_IU], fma2(v, dqy[E2D_IU], dqx[E2D_IP] * ir));
@@ -868,6 +877,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
       fx_prev[v] = fx[v];
       fy_prev[v] = fy[v];
     }
+    ib = ic;
     sm1 = wrap(sm1 + 1);
   }
   // the strip's fold-unit winners, one lane each, folded in parallel
