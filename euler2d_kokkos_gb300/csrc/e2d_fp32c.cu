@@ -125,13 +125,13 @@ __device__ __forceinline__ float max3f(float a, float b, float c) {
 // reference's form -- zero when (q-qm)*(qp-q) <= 0, else
 // sign(dcen) * min(st|q-qm|, st|qp-q|, |dcen|) -- is the minmod of the three
 // differences a = st(q-qm), b = st(qp-q), c = dcen:
-// max(0, min(a,b,c)) + min(0, max(a,b,c)).  When a and b have one sign, c
-// (half their sum) has it too and the minmod is the one of smallest
-// magnitude; when they differ both terms are 0.
+// the median of min(a,b,c), 0 and max(a,b,c), max(lo, min(hi, 0)).  When a
+// and b have one sign, c (half their sum) has it too and the minmod is the
+// one of smallest magnitude; when they differ it is 0.
 __device__ __forceinline__ float2 minmod2(float2 a, float2 b, float2 c) {
   const float2 lo = make_float2(min3f(a.x, b.x, c.x), min3f(a.y, b.y, c.y));
   const float2 hi = make_float2(max3f(a.x, b.x, c.x), max3f(a.y, b.y, c.y));
-  return max2(lo, f2(0.0f)) + min2(hi, f2(0.0f));
+  return max2(lo, min2(hi, f2(0.0f)));
 }
 // The slope divided by slope_type: minmod is homogeneous, so
 // minmod(st a, st b, c) = st minmod(a, b, c / st); the callers carry the
@@ -848,9 +848,10 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
           const float2 t = cfl_term2(k, idx, nh);
           const int loc = (m - 1 - rb) * 64 + 2 * lane + 1;
           // non-finite states: a NaN term never wins the arg-max, and the
-          // primitives' fmaxf cut-offs drop a NaN density or energy, so the
-          // new conserved values themselves are summed (tested at strip end)
-          float2 chk = (nh[0] + nh[1]) + (nh[2] + nh[3]);
+          // fmaxf cut-offs drop a NaN density or energy, so the new density
+          // and energy are summed with the term, which a non-finite momentum
+          // makes non-finite (tested at strip end)
+          float2 chk = (nh[0] + nh[1]) + t;
           if (!(c0 + 1 < g.nx + 2)) chk.y = 0.0f;  // a ghost column: not a cell of the grid
           nfacc = nfacc + chk;
           if (t.x > best) best = t.x, blocal = loc;

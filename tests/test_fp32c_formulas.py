@@ -1,8 +1,9 @@
 """Two rewritings of the FP32C step, checked in FP32 arithmetic on the CPU
 (numpy float32, the kernel's formulas restated):
 
-- the slope limiter as the minmod of three differences,
-  max(0, min(a, b, c)) + min(0, max(a, b, c)), against the reference's form
+- the slope limiter as slope_type times the minmod of q - qm, qp - q and
+  (qp - qm) / (2 slope_type), the minmod taken as the median of
+  min(a, b, c), 0 and max(a, b, c), against the reference's form
   (src/HydroBaseFunctor.h:421-455);
 - HLLC's sampling as one choice between a side's own state and its star
   state, which needs SL > 0 => u* > 0 and SR <= 0 => u* <= 0 for the wave
@@ -26,12 +27,13 @@ def reference_slope(q, qp, qm, st):
 
 
 def minmod_slope(q, qp, qm, st):
-    a = f32(st) * (q - qm)
-    b = f32(st) * (qp - q)
-    c = f32(0.5) * (qp - qm)
+    """The kernel's slope2 (the slope divided by st), times st."""
+    a = q - qm
+    b = qp - q
+    c = f32(0.5 / st) * (qp - qm)
     lo = np.minimum(np.minimum(a, b), c)
     hi = np.maximum(np.maximum(a, b), c)
-    return np.maximum(lo, f32(0)) + np.minimum(hi, f32(0))
+    return f32(st) * np.maximum(lo, np.minimum(hi, f32(0)))
 
 
 @pytest.mark.parametrize("st", [1.0, 2.0])
