@@ -285,8 +285,9 @@ int e2d_batch_stream(e2d_batch *b, void **stream);
  * blocks with rows staged through shared memory by cp.async; 6: 4 blocks,
  * rows staged by TMA copies waited on with mbarriers) and rows per strip (16..512,
  * rounded up to a multiple of 16) for the size classes max(nx, ny) <= 192,
- * <= 512, > 512.  Results do not depend on them.  e2d_batch_autotune times the candidates on the live
- * batch (its iterations advance the instances) and keeps the fastest. */
+ * <= 512, > 512.  Results do not depend on them.  e2d_batch_autotune times the staged variants (4, 5,
+ * 6) and then 16, 32 and 64 rows per size class on the live batch (its iterations advance the
+ * instances) and keeps the fastest. */
 int e2d_batch_set_tuning(e2d_batch *b, int variant, const int strip_h[3]);
 int e2d_batch_get_tuning(const e2d_batch *b, int *variant, int strip_h[3]);
 int e2d_batch_autotune(e2d_batch *b, int iters_per_trial);
