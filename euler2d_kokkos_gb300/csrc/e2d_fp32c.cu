@@ -547,8 +547,8 @@ __device__ __forceinline__ void stage_row_tma(const KGeom &g, const CUtensorMap 
 // kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
-template <int RS, int PFD, int TMA>
-__device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__restrict__ w_in,
+template <int RS, int PFD, int TMA, bool INTERIOR>
+__device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
                                             const int lane, unsigned long long *target,
@@ -569,7 +569,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   const int rb = 2 + sy * SH;         // array row of the strip's first output row
   const int re = min(rb + SH, g.ny + 2);
   const int c0 = cb - 2 + 2 * lane;   // the lane's columns: c0, c0 + 1
-  const bool direct = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1);
+  const bool direct = INTERIOR || ((cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1));
   const bool writer = (lane >= 1) && (lane <= 30) && (c0 < g.nx + 2);
   const C2 k = make_c2(ph);
   const float2 idx = make_float2(1.0f / ph.dx, 1.0f / ph.dy);
@@ -595,7 +595,7 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   }
   constexpr int R = PFD + 3;  // ring slots; row r sits in slot (r - rb + 2) mod R
   static_assert(TMA != 2 || R == 6, "row pairs need a ring of three pairs");
-  const bool yghost = (rb - 2 < 2) || (re + 1 > g.ny + 1);
+  const bool yghost = !INTERIOR && ((rb - 2 < 2) || (re + 1 > g.ny + 1));
   // Staged variants: interior strips (`bulk`) fill the ring by TMA copies
   // and wait on the slots' barriers; boundary strips copy each lane's
   // boundary-mapped columns by cp.async and wait on commit groups.  With
@@ -894,6 +894,27 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
     }
   }
   return true;
+}
+
+// Interior strips (every column and row they read is a cell of the grid:
+// no boundary map, no ghost flips) run an instantiation with those tests
+// folded away; the others run the general one.  Same arithmetic, same bits.
+template <int RS, int PFD, int TMA>
+__device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__restrict__ w_in,
+                                            float *__restrict__ w_out, const float2 dtdx,
+                                            const float2 dtdy, const int sx, const int sy,
+                                            const int lane, unsigned long long *target,
+                                            unsigned int *status, float *ring, const CUtensorMap *map,
+                                            unsigned long long *bars, unsigned int &phase) {
+  const KGeom &g = kp.g;
+  const int cb = 2 + sx * OUTW, rb = 2 + sy * kp.strip_h;
+  const int re = min(rb + kp.strip_h, g.ny + 2);
+  const bool interior = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1) && !(rb - 2 < 2) && !(re + 1 > g.ny + 1);
+  if (interior)
+    return march_strip_t<RS, PFD, TMA, true>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status, ring, map,
+                                             bars, phase);
+  return march_strip_t<RS, PFD, TMA, false>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status, ring, map,
+                                            bars, phase);
 }
 
 extern __shared__ __align__(16) float g_ring[];
