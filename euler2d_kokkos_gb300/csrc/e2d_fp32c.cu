@@ -547,7 +547,7 @@ __device__ __forceinline__ void stage_row_tma(const KGeom &g, const CUtensorMap 
 // kernel or the batch (strip_h must be a multiple of CFL_UNIT_ROWS and at
 // most 32 units).  Each unit's FP32 arg-max is parked in lane `unit`; the
 // parked winners are recomputed in FP64 together when the strip ends.
-template <int RS, int PFD, int TMA, bool INTERIOR>
+template <int RS, int PFD, int TMA, bool INTERIOR, bool TGT>
 __device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
                                             const float2 dtdy, const int sx, const int sy,
@@ -844,7 +844,7 @@ __device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *
           *reinterpret_cast<float2 *>(w_out + base + (4 + v) * kp.wplane) = l2;
           nh[v] = h2;
         }
-        if (target) {
+        if (TGT || target) {
           const float2 t = cfl_term2(k, idx, nh);
           const int loc = (m - 1 - rb) * 64 + 2 * lane + 1;
           // non-finite states: a NaN term never wins the arg-max, and the
@@ -860,7 +860,7 @@ __device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *
       }
       const int r = m - 1;  // >= rb >= 2, so the low bits of r - 2 are its remainder
       static_assert((CFL_UNIT_ROWS & (CFL_UNIT_ROWS - 1)) == 0, "fold units are a power of two rows");
-      if (target && (((r - 2) & (CFL_UNIT_ROWS - 1)) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
+      if ((TGT || target) && (((r - 2) & (CFL_UNIT_ROWS - 1)) == CFL_UNIT_ROWS - 1 || r == re - 1)) {
         float ut;
         const int win = unit_argmax(best, blocal, &ut);
         if (lane == unit) pend_term = ut, pend_local = win;
@@ -882,7 +882,7 @@ __device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *
     sm1 = wrap(sm1 + 1);
   }
   // the strip's fold-unit winners, one lane each, folded in parallel
-  if (target) {
+  if (TGT || target) {
     const float kInf = __int_as_float(0x7f800000);
     const bool nonfin = !(fabsf(nfacc.x) < kInf) || !(fabsf(nfacc.y) < kInf);
     if (__any_sync(0xffffffffu, nonfin) && lane == 0) atomicOr(status, (unsigned)E2D_FLAG_NONFINITE);
@@ -897,8 +897,10 @@ __device__ __forceinline__ bool march_strip_t(const KParams32 &kp, const float *
 }
 
 // Interior strips (every column and row they read is a cell of the grid:
-// no boundary map, no ghost flips) run an instantiation with those tests
-// folded away; the others run the general one.  Same arithmetic, same bits.
+// no boundary map, no ghost flips) of the staged variants that fold the CFL
+// maximum (every step of the device loop and of a batch) run an
+// instantiation with those tests folded away; the others run the general
+// one.  Same arithmetic, same bits.
 template <int RS, int PFD, int TMA>
 __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__restrict__ w_in,
                                             float *__restrict__ w_out, const float2 dtdx,
@@ -910,11 +912,13 @@ __device__ __forceinline__ bool march_strip(const KParams32 &kp, const float *__
   const int cb = 2 + sx * OUTW, rb = 2 + sy * kp.strip_h;
   const int re = min(rb + kp.strip_h, g.ny + 2);
   const bool interior = (cb - 2 >= 2) && (cb + OUTW + 1 <= g.nx + 1) && !(rb - 2 < 2) && !(re + 1 > g.ny + 1);
-  if (interior)
-    return march_strip_t<RS, PFD, TMA, true>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status, ring, map,
-                                             bars, phase);
-  return march_strip_t<RS, PFD, TMA, false>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status, ring, map,
-                                            bars, phase);
+  if constexpr (PFD > 0) {
+    if (interior && target)
+      return march_strip_t<RS, PFD, TMA, true, true>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status,
+                                                     ring, map, bars, phase);
+  }
+  return march_strip_t<RS, PFD, TMA, false, false>(kp, w_in, w_out, dtdx, dtdy, sx, sy, lane, target, status,
+                                                   ring, map, bars, phase);
 }
 
 extern __shared__ __align__(16) float g_ring[];
