@@ -1060,9 +1060,13 @@ __global__ void __launch_bounds__(NT, MINB)
     const int par = I.par;
     const int strip = w - strip_begin[lo];
     if (ring_ok) {
-      ring_ok = march_strip<RS, PFD, TMA>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy), strip % I.nsx,
-                                          strip / I.nsx, lane, &I.acc[(I.nstep + 1) & 1], &I.status,
-                                          warp_ring<PFD>(threadIdx.x >> 5), &I.tm[par], bars, phase);
+      // the general march only: a persistent warp takes strips of many
+      // instances, mostly boundary strips of small grids, and a second
+      // instantiation in this loop measured 14 % slower on the 512-solve mix
+      ring_ok = march_strip_t<RS, PFD, TMA, false, false>(kp, I.w[par], I.w[par ^ 1], f2(I.dtdx), f2(I.dtdy),
+                                                          strip % I.nsx, strip / I.nsx, lane,
+                                                          &I.acc[(I.nstep + 1) & 1], &I.status,
+                                                          warp_ring<PFD>(threadIdx.x >> 5), &I.tm[par], bars, phase);
     } else if (lane == 0) {
       // a copy of an abandoned strip may still land in this warp's ring:
       // its remaining strips are not computed, their instances stop
